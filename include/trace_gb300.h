@@ -1,0 +1,177 @@
+/* trace_gb300 — GB300 (sm_103a) implementation of Trace's iterative
+ * reconstruction hot path behind a plain C ABI.
+ *
+ * One plan holds one parallel-beam geometry (num_projs angles x num_cols
+ * detector columns, grid = num_cols), the sinogram of num_slices slices, the
+ * reconstruction, and the device-resident system matrix traced once from the
+ * geometry. Calls replace, for that path, the reference's operator surface:
+ *
+ *   reference (file:line in tekinbicer/Trace)          replaced by
+ *   ------------------------------------------------   --------------------------
+ *   TraceMetadata ctor, src/common/trace_data.h:53-109  tg_plan_create
+ *   DataRegionBase over the sinogram,
+ *     src/common/DISP/core/data_region_base.h:48-51    tg_set_sinogram
+ *   trace_utils::Absolute, src/common/trace_utils.cc:4-8  tg_set_sinogram(abs=1)
+ *   trace_utils::DegreeToRadian, trace_utils.cc:10-24   tg_degree_to_radian
+ *   trace_utils::Calculate* tracer chain,
+ *     src/common/trace_utils.cc:41-216                  tg_trace_rays (export)
+ *   DISPEngineReduction::RunParallelReduction +
+ *     XReconSpace::Reduce (sirt.cc:97-186, mlem.cc:92-181,
+ *     pml.cc:276-366, apmlr.cc:1057-1147)               tg_reduce
+ *   ParInPlaceLocalSynchWrapper,
+ *     disp_engine_reduction.h:132-167                   (no-op: one device replica)
+ *   XReconSpace::reduction_objects(),
+ *     reduction_space_a.h:40-42                         tg_get_replica
+ *   PMLReconSpace::CalculateFG pml.cc:25-201 /
+ *     APMLRReconSpace::CalculateFG apmlr.cc:919-982     tg_calculate_fg
+ *   XReconSpace::UpdateRecon sirt.cc:21-33, mlem.cc:21-34,
+ *     pml.cc:3-23, apmlr.cc:3-26                        tg_update_recon
+ *   ResetReductionSpaces, disp_engine_reduction.h:188-202  tg_reset_replica
+ *   the drivers' iteration loop, e.g.
+ *     src/sirt/sirt_main.cc:177-202                     tg_iterate (fused)
+ *   TraceMetadata::recon(), trace_data.h:169            tg_get_recon / tg_set_recon
+ *
+ * Conventions: every function returns 0 on success or a TG_E* code; the
+ * message of the last failure on a plan is tg_last_error(plan) (or
+ * tg_last_error(NULL) for a failed tg_plan_create). No call throws. The
+ * library owns device memory; callers own host buffers. Each plan issues its
+ * work on one CUDA stream (its own, or one given with tg_plan_set_stream).
+ * Calls on one plan are not thread-safe; distinct plans are independent.
+ */
+#ifndef TRACE_GB300_H
+#define TRACE_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TG_ABI_VERSION 1
+
+enum tg_status {
+  TG_OK = 0,
+  TG_E_ARG = 1,      /* invalid argument (null pointer, bad size, bad enum) */
+  TG_E_CUDA = 2,     /* a CUDA runtime call failed */
+  TG_E_NOMEM = 3,    /* device allocation failed */
+  TG_E_STATE = 4,    /* call out of order (e.g. no sinogram uploaded) */
+  TG_E_GEOMETRY = 5, /* geometry outside what the plan's layout supports */
+  TG_E_LIMIT = 6     /* request exceeds a fixed limit of the entry point */
+};
+
+enum tg_alg { TG_SIRT = 0, TG_MLEM = 1, TG_PML = 2, TG_APMLR = 3 };
+
+/* Storage of the traced segment lengths in the device system matrix.
+ * Arithmetic is FP32 in every case. */
+enum tg_len_storage {
+  TG_LEN_F32 = 0,  /* float32 lengths */
+  TG_LEN_BF16 = 1, /* bfloat16 */
+  TG_LEN_F16 = 2,  /* IEEE half */
+  TG_LEN_U16 = 3   /* 16-bit fixed point, scale = longest segment / 65535 */
+};
+
+/* Arithmetic mode of the iteration kernels. */
+enum tg_mode {
+  TG_MODE_EXACT = 0, /* reference operation order, IEEE-rounded mul/add/div:
+                        forward ray sums are bit-identical to the reference */
+  TG_MODE_FAST = 1   /* fused multiply-add and compensated (Kahan) sums */
+};
+
+typedef struct {
+  int num_projs;          /* P: angles */
+  int num_slices;         /* S: sinogram slices held by this plan */
+  int num_cols;           /* C: detector columns; the grid is C x C */
+  float center;           /* rotation centre; <= 0 selects C/2 + 1 */
+  int slice_id;           /* global index of this plan's first slice */
+  int num_total_slices;   /* slices in the whole dataset (APMLR top/bottom) */
+  int len_storage;        /* tg_len_storage */
+  int slices_per_pass;    /* k in {1,2,4,8}: slices served per matrix read */
+  int mode;               /* tg_mode */
+  int delta_index;        /* 1 = forward pixel indices delta-coded (4 bits) */
+  int apmlr_fixed_offset; /* APMLR only. 0 = reference behaviour: the forward
+                             projection of slice s reads reconstruction slice
+                             s-1 (apmlr.cc:1083-1084); 1 = reads slice s */
+} tg_plan_desc;
+
+typedef struct {
+  float beta;    /* PML beta; APMLR in-plane beta0 */
+  float beta1;   /* APMLR axial beta */
+  float delta;   /* APMLR in-plane delta0 */
+  float delta1;  /* APMLR axial delta */
+  float regw;    /* APMLR axial weight */
+} tg_params;
+
+typedef struct {
+  int64_t num_segments;       /* traced ray-pixel segments (one slice) */
+  int64_t forward_bytes;      /* bytes of the forward (ray-major) matrix */
+  int64_t backward_bytes;     /* bytes of the backward (pixel-major) matrix */
+  int64_t device_bytes;       /* all device memory held by the plan */
+  float max_segment_length;
+  double setup_ms;            /* time spent tracing and building matrices */
+  int batches;                /* ceil(stored slices / slices_per_pass) */
+} tg_plan_info;
+
+typedef struct tg_plan tg_plan;
+
+int tg_abi_version(void);
+
+/* Create a plan: traces every ray of the geometry on the device and builds
+ * the forward and backward matrices. theta (P floats, radians) is required.
+ * sin_tab / cos_tab (P floats each, both or neither) replace the host
+ * C library's sinf/cosf values the reference uses (sirt.cc:119-120). */
+int tg_plan_create(const tg_plan_desc* desc, const float* theta,
+                   const float* sin_tab, const float* cos_tab, tg_plan** out);
+int tg_plan_destroy(tg_plan* plan);
+int tg_plan_get_info(const tg_plan* plan, tg_plan_info* info);
+/* Use `stream` (a cudaStream_t) for all later work of this plan; NULL
+ * returns to the plan's own stream. */
+int tg_plan_set_stream(tg_plan* plan, void* stream);
+int tg_synchronize(tg_plan* plan);
+const char* tg_last_error(const tg_plan* plan);
+
+/* In-place degrees -> radians with the reference's float constant. Host. */
+int tg_degree_to_radian(float* theta, int n);
+
+/* Sinogram in the reference layout [P][S][C] float32. `on_device` != 0 means
+ * `sino` is a device pointer. apply_abs != 0 applies |x| (trace_utils::Absolute)
+ * during the upload. */
+int tg_set_sinogram(tg_plan* plan, const float* sino, int on_device,
+                    int apply_abs);
+
+/* Reconstruction in the reference layout: (S + 2*halo) x C x C float32 where
+ * halo = 1 for APMLR (TraceMetadata with num_neighbor_recon_slices = 1) and 0
+ * otherwise. tg_reset_recon fills it with the algorithm's initial value
+ * (0 for SIRT, 1 otherwise; trace_data.h:91-94 with the drivers' init). */
+int tg_reset_recon(tg_plan* plan, int alg);
+int tg_set_recon(tg_plan* plan, int alg, const float* recon, int on_device);
+int tg_get_recon(tg_plan* plan, int alg, float* recon, int on_device);
+
+/* Operator-level surface (one call per reference engine step). */
+int tg_reduce(tg_plan* plan, int alg, const tg_params* params);
+int tg_get_replica(tg_plan* plan, int alg, float* replica /* S x 2*C*C */,
+                   int on_device);
+int tg_calculate_fg(tg_plan* plan, int alg, const tg_params* params);
+int tg_get_fg(tg_plan* plan, float* F, float* G /* S x C x C each */,
+              int on_device);
+int tg_update_recon(tg_plan* plan, int alg, const tg_params* params);
+int tg_reset_replica(tg_plan* plan);
+
+/* Fused iterations: forward projection + backprojection + (penalty) update
+ * per slice batch, n_iter times. */
+int tg_iterate(tg_plan* plan, int alg, const tg_params* params, int n_iter);
+
+/* Forward projection of the current reconstruction: sim [P][S][C]. */
+int tg_forward_project(tg_plan* plan, int alg, const tg_params* params,
+                       float* sim, int on_device);
+
+/* Traced segment lists in the reference's order, ray r = p*C + c.
+ * counts: P*C ints. With idx == NULL only counts are written; otherwise
+ * offsets (P*C+1, exclusive scan of counts) must be given and idx/len
+ * (and len2, nullable) receive the segments. Host buffers. */
+int tg_trace_rays(tg_plan* plan, int32_t* counts, const int64_t* offsets,
+                  int32_t* idx, float* len, float* len2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TRACE_GB300_H */

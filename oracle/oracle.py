@@ -228,3 +228,40 @@ def ref_run(alg, sino, theta, *, n_iter=1, center=0.0, threads=1, beta=10.0,
        C.c_int(slice_id), C.c_int(S if num_total_slices is None else num_total_slices),
        C.c_int(apply_abs), _ptr(out), _ptr(iters), _ptr(rep))
     return {"recon": out, "iters": iters, "replica": rep}
+
+
+def forward(recon, tables, center=0.0, threads=8):
+    """Sequential-float forward projection: sim [P][S][C] of recon [S][C][C]."""
+    recon = np.ascontiguousarray(recon, np.float32)
+    S, Cn, _ = recon.shape
+    s, c, q = (np.ascontiguousarray(t) for t in tables)
+    P = s.size
+    sim = np.empty((P, S, Cn), np.float32)
+    rc = port().tor_forward(C.c_int(Cn), C.c_int(P), C.c_int(S), C.c_float(center),
+                            _ptr(s), _ptr(c), _ptr(q), _ptr(recon), _ptr(sim),
+                            C.c_int(threads))
+    if rc:
+        raise ValueError("tor_forward failed")
+    return sim
+
+
+def fg(alg, recon, W, *, beta=10.0, beta1=1.0, delta=1.0, delta1=1.0, regw=1.0,
+       slice_id=0, num_total_slices=None):
+    """F and G as CalculateFG leaves them. recon includes APMLR's halo slices."""
+    if isinstance(alg, str):
+        alg = ALGS[alg]
+    recon = np.ascontiguousarray(recon, np.float32)
+    halo = 1 if alg == APMLR else 0
+    S = recon.shape[0] - 2 * halo
+    Cn = recon.shape[1]
+    W = np.ascontiguousarray(W, np.float32)
+    F = np.empty((S, Cn, Cn), np.float32)
+    G = np.empty_like(F)
+    rc = port().tor_fg(C.c_int(alg), C.c_int(S), C.c_int(Cn), _ptr(recon), _ptr(W),
+                       C.c_float(beta), C.c_float(beta1), C.c_float(delta),
+                       C.c_float(delta1), C.c_float(regw), C.c_int(slice_id),
+                       C.c_int(S if num_total_slices is None else num_total_slices),
+                       _ptr(F), _ptr(G))
+    if rc:
+        raise ValueError("tor_fg failed")
+    return F, G

@@ -513,6 +513,64 @@ int tor_run(const tor_run_args* a) {
   return Run<double>(*a).run();
 }
 
+int tor_forward(int num_cols, int num_projs, int num_slices, float center,
+                const float* sinq, const float* cosq, const int32_t* quad,
+                const float* recon, float* sim, int threads) {
+  if (num_cols < 2 || num_projs < 1 || num_slices < 1) return 1;
+  Geometry G;
+  make_geometry(G, num_cols, num_projs, center, nullptr, sinq, cosq, quad);
+  const size_t g2 = (size_t)num_cols * num_cols;
+  parallel_for((long)num_projs, threads, [&](long p, int) {
+    std::vector<Seg> buf;
+    for (int c = 0; c < num_cols; ++c) {
+      buf.clear();
+      trace_ray(G, (int)p, c, [&](const Seg& sg) { buf.push_back(sg); });
+      for (int s = 0; s < num_slices; ++s) {
+        const float* rc = recon + (size_t)s * g2;
+        float acc = 0.f;
+        for (const Seg& sg : buf) acc += rc[sg.idx] * sg.len;
+        sim[((size_t)p * num_slices + s) * num_cols + c] = acc;
+      }
+    }
+  });
+  return 0;
+}
+
+int tor_fg(int alg, int num_slices, int num_cols, const float* recon,
+           const float* W, float beta, float beta1, float delta, float delta1,
+           float regw, int slice_id, int num_total_slices, float* F, float* G) {
+  if ((alg != TOR_PML && alg != TOR_APMLR) || num_cols < 2 || num_slices < 1)
+    return 1;
+  tor_run_args a{};
+  a.alg = alg;
+  a.precision = TOR_F32;
+  a.num_projs = 1;
+  a.num_slices = num_slices;
+  a.num_cols = num_cols;
+  const float th = 0.f;
+  a.theta = &th;
+  std::vector<float> dummy((size_t)num_slices * num_cols, 0.f);
+  a.sino = dummy.data();
+  a.beta = beta;
+  a.beta1 = beta1;
+  a.delta = delta;
+  a.delta1 = delta1;
+  a.regw = regw;
+  a.slice_id = slice_id;
+  a.num_total_slices = num_total_slices;
+  a.recon_in = recon;
+  Run<float> run(a);
+  const size_t g2 = (size_t)num_cols * num_cols;
+  std::vector<float> rep((size_t)num_slices * 2 * g2, 0.f);
+  for (int k = 0; k < num_slices; ++k)
+    for (size_t j = 0; j < g2; ++j) rep[(size_t)k * 2 * g2 + 2 * j + 1] = W[j];
+  std::vector<float> Fv, Gv;
+  run.calculate_fg(rep, Fv, Gv);
+  std::memcpy(F, Fv.data(), Fv.size() * sizeof(float));
+  std::memcpy(G, Gv.data(), Gv.size() * sizeof(float));
+  return 0;
+}
+
 double tor_last_loop_seconds(void) { return g_last_loop_seconds; }
 
 }  // extern "C"

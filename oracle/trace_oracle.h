@@ -70,6 +70,20 @@ typedef struct {
 
 int tor_run(const tor_run_args* a);
 
+/* Forward projection in the reference's order (CalculateSimdata,
+ * sirt.cc:4-19): sim[p][s][c] = sum over ray (p,c) of recon[s][idx]*len,
+ * accumulated sequentially in float. recon: S x C x C. */
+int tor_forward(int num_cols, int num_projs, int num_slices, float center,
+                const float* sinq, const float* cosq, const int32_t* quad,
+                const float* recon, float* sim, int threads);
+
+/* F and G of PML / APMLR for a given reconstruction (including APMLR's
+ * halo slices: S + 2 slices) and per-pixel total length W (C x C), exactly
+ * as CalculateFG leaves them (G includes W). F, G: S x C x C. */
+int tor_fg(int alg, int num_slices, int num_cols, const float* recon,
+           const float* W, float beta, float beta1, float delta, float delta1,
+           float regw, int slice_id, int num_total_slices, float* F, float* G);
+
 /* Seconds spent in the last tor_run's iteration loop (reduction + combine +
  * FG + update), the span the reference drivers' timers cover. */
 double tor_last_loop_seconds(void);

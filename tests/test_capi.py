@@ -1,0 +1,86 @@
+"""The C-ABI library: builds for sm_103a, loads, exports every declared
+symbol, validates arguments on the host, and fails loudly without a GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import trace_gb300 as tg
+from trace_gb300 import build as tgb
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "trace_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(tg_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    tgb.build()
+    return tg.load_library()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(tg.EXPORTED) <= set(syms)
+
+
+def test_abi_version(lib):
+    assert lib.tg_abi_version() == 1
+
+
+def test_degree_to_radian_matches_reference_formula(lib):
+    deg = np.linspace(0, 359, 181).astype(np.float32)
+    got = tg.degree_to_radian(deg)
+    kpi = np.float32(3.14159265358979)
+    want = ((deg * kpi).astype(np.float64) / 180.0).astype(np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def _desc(**kw):
+    d = dict(num_projs=10, num_slices=2, num_cols=16, center=0.0, slice_id=0,
+             num_total_slices=2, len_storage=0, slices_per_pass=1, mode=0,
+             delta_index=0, apmlr_fixed_offset=0)
+    d.update(kw)
+    return tg.PlanDesc(**d)
+
+
+@pytest.mark.parametrize("bad", [dict(num_cols=1), dict(num_projs=0),
+                                 dict(slices_per_pass=3), dict(len_storage=9),
+                                 dict(mode=5), dict(num_slices=0)])
+def test_invalid_descriptors_rejected_on_host(lib, bad):
+    theta = np.zeros(10, np.float32)
+    h = C.c_void_p()
+    rc = lib.tg_plan_create(C.byref(_desc(**bad)), theta.ctypes.data_as(C.c_void_p),
+                            None, None, C.byref(h))
+    assert rc == 1
+    assert lib.tg_last_error(None)
+    assert not h.value
+
+
+def test_null_arguments_rejected(lib):
+    assert lib.tg_plan_create(None, None, None, None, None) == 1
+    assert lib.tg_iterate(None, 0, None, 1) == 1
+    assert lib.tg_set_sinogram(None, None, 0, 0) == 1
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-GPU failure path")
+def test_plan_creation_fails_loudly_without_gpu(lib):
+    with pytest.raises(tg.TraceError) as e:
+        tg.Plan(8, 1, 16, np.zeros(8, np.float32))
+    assert "CUDA" in str(e.value) or "E_CUDA" in str(e.value)

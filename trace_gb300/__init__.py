@@ -1,0 +1,279 @@
+"""trace_gb300: GB300-native iterative reconstruction hot path of Trace.
+
+Python host binding over the C ABI in ``include/trace_gb300.h``. The compute
+runs only in the in-tree CUDA library ``trace_gb300/_build/libtrace_gb300.so``;
+there is no CPU fallback: importing the bindings without the library raises.
+
+Typical use (mirrors a reference driver's loop, e.g. src/sirt/sirt_main.cc):
+
+    plan = Plan(num_projs=P, num_slices=S, num_cols=C, theta=theta)
+    plan.set_sinogram(sino)            # [P][S][C] float32
+    plan.reset_recon("sirt")
+    plan.iterate("sirt", n_iter=10)
+    recon = plan.get_recon("sirt")     # [S][C][C]
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import LIB as LIB_PATH
+
+ALGS = {"sirt": 0, "mlem": 1, "pml": 2, "apmlr": 3}
+LEN_STORAGE = {"f32": 0, "bf16": 1, "f16": 2, "u16": 3}
+MODES = {"exact": 0, "fast": 1}
+STATUS = {0: "OK", 1: "E_ARG", 2: "E_CUDA", 3: "E_NOMEM", 4: "E_STATE",
+          5: "E_GEOMETRY", 6: "E_LIMIT"}
+
+EXPORTED = [
+    "tg_abi_version", "tg_plan_create", "tg_plan_destroy", "tg_plan_get_info",
+    "tg_plan_set_stream", "tg_synchronize", "tg_last_error",
+    "tg_degree_to_radian", "tg_set_sinogram", "tg_reset_recon", "tg_set_recon",
+    "tg_get_recon", "tg_reduce", "tg_get_replica", "tg_calculate_fg",
+    "tg_get_fg", "tg_update_recon", "tg_reset_replica", "tg_iterate",
+    "tg_forward_project", "tg_trace_rays",
+]
+
+
+class TraceError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class PlanDesc(C.Structure):
+    _fields_ = [("num_projs", C.c_int), ("num_slices", C.c_int),
+                ("num_cols", C.c_int), ("center", C.c_float),
+                ("slice_id", C.c_int), ("num_total_slices", C.c_int),
+                ("len_storage", C.c_int), ("slices_per_pass", C.c_int),
+                ("mode", C.c_int), ("delta_index", C.c_int),
+                ("apmlr_fixed_offset", C.c_int)]
+
+
+class Params(C.Structure):
+    _fields_ = [("beta", C.c_float), ("beta1", C.c_float), ("delta", C.c_float),
+                ("delta1", C.c_float), ("regw", C.c_float)]
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [("num_segments", C.c_int64), ("forward_bytes", C.c_int64),
+                ("backward_bytes", C.c_int64), ("device_bytes", C.c_int64),
+                ("max_segment_length", C.c_float), ("setup_ms", C.c_double),
+                ("batches", C.c_int)]
+
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Load the CUDA library (built by ``trace_gb300.build``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"trace_gb300 CUDA library not built ({path}); run "
+            "`python -m trace_gb300.build` (there is no CPU fallback)")
+    lib = C.CDLL(path)
+    vp = C.c_void_p
+    lib.tg_last_error.restype = C.c_char_p
+    lib.tg_last_error.argtypes = [vp]
+    lib.tg_plan_create.argtypes = [C.POINTER(PlanDesc), vp, vp, vp, C.POINTER(vp)]
+    for name in EXPORTED:
+        getattr(lib, name)  # every declared symbol must exist
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(C.c_void_p)
+    if hasattr(a, "data_ptr"):  # torch tensor on the device
+        return C.c_void_p(a.data_ptr())
+    return C.c_void_p(int(a))
+
+
+def _is_device(a):
+    return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
+
+
+def default_params(alg: str, beta=None, beta1=1.0, delta=1.0, delta1=1.0,
+                   regw=1.0) -> Params:
+    """Reference defaults: PML beta 10 (pml_main.cc:20), APMLR beta0=10,
+    beta1=1, delta0=1, delta1=1, regw=1 (apmlr_main.cc:22-26)."""
+    return Params(10.0 if beta is None else beta, beta1, delta, delta1, regw)
+
+
+class Plan:
+    """One geometry + sinogram + reconstruction on the device."""
+
+    def __init__(self, num_projs, num_slices, num_cols, theta, *, center=0.0,
+                 len_storage="f32", slices_per_pass=1, mode="exact",
+                 delta_index=False, apmlr_fixed_offset=False, slice_id=0,
+                 num_total_slices=None, sin_tab=None, cos_tab=None):
+        self._lib = load_library()
+        self.P, self.S, self.C = int(num_projs), int(num_slices), int(num_cols)
+        d = PlanDesc(self.P, self.S, self.C, float(center), int(slice_id),
+                     int(num_total_slices or num_slices),
+                     LEN_STORAGE[len_storage] if isinstance(len_storage, str) else int(len_storage),
+                     int(slices_per_pass),
+                     MODES[mode] if isinstance(mode, str) else int(mode),
+                     int(bool(delta_index)), int(bool(apmlr_fixed_offset)))
+        theta = np.ascontiguousarray(theta, np.float32)
+        if theta.size != self.P:
+            raise ValueError("theta must have num_projs entries")
+        st = ct = None
+        if sin_tab is not None:
+            st = np.ascontiguousarray(sin_tab, np.float32)
+            ct = np.ascontiguousarray(cos_tab, np.float32)
+        h = C.c_void_p()
+        rc = self._lib.tg_plan_create(C.byref(d), _ptr(theta), _ptr(st), _ptr(ct),
+                                      C.byref(h))
+        if rc != 0:
+            raise TraceError(rc, self._lib.tg_last_error(None).decode())
+        self._h = h
+
+    # -- plumbing
+    def _chk(self, rc):
+        if rc != 0:
+            raise TraceError(rc, self._lib.tg_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.tg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> dict:
+        i = PlanInfo()
+        self._chk(self._lib.tg_plan_get_info(self._h, C.byref(i)))
+        return {f: getattr(i, f) for f, _ in PlanInfo._fields_}
+
+    def set_stream(self, stream_ptr):
+        self._chk(self._lib.tg_plan_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    def synchronize(self):
+        self._chk(self._lib.tg_synchronize(self._h))
+
+    @staticmethod
+    def _alg(alg):
+        return ALGS[alg] if isinstance(alg, str) else int(alg)
+
+    def halo(self, alg):
+        return 1 if self._alg(alg) == 3 else 0
+
+    # -- data
+    def set_sinogram(self, sino, apply_abs=False):
+        if _is_device(sino):
+            self._chk(self._lib.tg_set_sinogram(self._h, _ptr(sino), 1, int(apply_abs)))
+            return
+        sino = np.ascontiguousarray(sino, np.float32)
+        if sino.shape != (self.P, self.S, self.C):
+            raise ValueError(f"sinogram must be [P][S][C] = {(self.P, self.S, self.C)}")
+        self._chk(self._lib.tg_set_sinogram(self._h, _ptr(sino), 0, int(apply_abs)))
+
+    def reset_recon(self, alg):
+        self._chk(self._lib.tg_reset_recon(self._h, self._alg(alg)))
+
+    def set_recon(self, alg, recon):
+        if _is_device(recon):
+            self._chk(self._lib.tg_set_recon(self._h, self._alg(alg), _ptr(recon), 1))
+            return
+        recon = np.ascontiguousarray(recon, np.float32)
+        n = self.S + 2 * self.halo(alg)
+        if recon.shape != (n, self.C, self.C):
+            raise ValueError(f"recon must be {(n, self.C, self.C)}")
+        self._chk(self._lib.tg_set_recon(self._h, self._alg(alg), _ptr(recon), 0))
+
+    def get_recon(self, alg, out=None):
+        if out is not None and _is_device(out):
+            self._chk(self._lib.tg_get_recon(self._h, self._alg(alg), _ptr(out), 1))
+            return out
+        n = self.S + 2 * self.halo(alg)
+        out = np.empty((n, self.C, self.C), np.float32)
+        self._chk(self._lib.tg_get_recon(self._h, self._alg(alg), _ptr(out), 0))
+        return out
+
+    # -- operators
+    def iterate(self, alg, n_iter=1, params=None):
+        p = params if params is not None else default_params(alg)
+        self._chk(self._lib.tg_iterate(self._h, self._alg(alg), C.byref(p), int(n_iter)))
+
+    def reduce(self, alg, params=None):
+        p = params if params is not None else default_params(alg)
+        self._chk(self._lib.tg_reduce(self._h, self._alg(alg), C.byref(p)))
+
+    def get_replica(self, alg):
+        out = np.empty((self.S, 2 * self.C * self.C), np.float32)
+        self._chk(self._lib.tg_get_replica(self._h, self._alg(alg), _ptr(out), 0))
+        return out
+
+    def calculate_fg(self, alg, params=None):
+        p = params if params is not None else default_params(alg)
+        self._chk(self._lib.tg_calculate_fg(self._h, self._alg(alg), C.byref(p)))
+
+    def get_fg(self):
+        F = np.empty((self.S, self.C, self.C), np.float32)
+        G = np.empty_like(F)
+        self._chk(self._lib.tg_get_fg(self._h, _ptr(F), _ptr(G), 0))
+        return F, G
+
+    def update_recon(self, alg, params=None):
+        p = params if params is not None else default_params(alg)
+        self._chk(self._lib.tg_update_recon(self._h, self._alg(alg), C.byref(p)))
+
+    def reset_replica(self):
+        self._chk(self._lib.tg_reset_replica(self._h))
+
+    def forward_project(self, alg="sirt", out=None):
+        p = default_params(alg)
+        if out is not None and _is_device(out):
+            self._chk(self._lib.tg_forward_project(self._h, self._alg(alg), C.byref(p), _ptr(out), 1))
+            return out
+        out = np.empty((self.P, self.S, self.C), np.float32)
+        self._chk(self._lib.tg_forward_project(self._h, self._alg(alg), C.byref(p), _ptr(out), 0))
+        return out
+
+    def trace_rays(self):
+        """(counts, offsets, idx, len, len2) of every ray, r = p*C + c."""
+        R = self.P * self.C
+        counts = np.empty(R, np.int32)
+        self._chk(self._lib.tg_trace_rays(self._h, _ptr(counts), None, None, None, None))
+        offs = np.zeros(R + 1, np.int64)
+        np.cumsum(counts, out=offs[1:])
+        n = int(offs[-1])
+        idx = np.empty(n, np.int32)
+        ln = np.empty(n, np.float32)
+        ln2 = np.empty(n, np.float32)
+        self._chk(self._lib.tg_trace_rays(self._h, _ptr(counts), _ptr(offs), _ptr(idx),
+                                          _ptr(ln), _ptr(ln2)))
+        return counts, offs, idx, ln, ln2
+
+
+def degree_to_radian(theta):
+    t = np.ascontiguousarray(theta, np.float32).copy()
+    lib = load_library()
+    rc = lib.tg_degree_to_radian(_ptr(t), C.c_int(t.size))
+    if rc:
+        raise TraceError(rc, "bad theta")
+    return t

@@ -1,0 +1,205 @@
+// Device-side building blocks shared by the trace_gb300 kernels: rounding-
+// explicit float arithmetic, segment-length codecs, the parallel-beam ray
+// tracer, and the (pixel, angle) ray window of the backward matrix.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tg {
+
+// ---- IEEE single operations that the compiler may not contract ------------
+// The reference is compiled for x86-64 without FMA, so each of its float
+// multiplies and adds rounds separately. These wrappers pin that.
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+
+// ---- geometry ---------------------------------------------------------------
+struct DevGeom {
+  int C;        // detector columns == grid size g
+  int P;        // angles
+  int gpa;      // ray groups (of 32 columns) per angle
+  int gpr;      // pixel groups (of 32 columns) per grid row
+  float halfg;  // g/2 (exact)
+  float mgrids; // (float)(g/2.) as trace_utils.cc:170
+  float off;    // (1-C)/2 + mov: detector offset of column 0
+  const float* yi;    // [C] source-frame offset per column (sirt.cc:129)
+  const float* sinq;  // [P]
+  const float* cosq;  // [P]
+  const int* quad;    // [P]
+};
+
+// Grid line n (gridx == gridy), -g/2 + n: exact in float for g < 2^23.
+__device__ __forceinline__ float grid_line(const DevGeom& G, int n) {
+  return fsub((float)n, G.halfg);
+}
+
+// Streams the segments of ray (a, c) to emit(idx, len, len2) in the order of
+// the reference tracer (trace_utils.cc:48-216 composed as sirt.cc:126-160).
+// Returns the segment count max(len-1, 0).
+//
+// Crossings with horizontal grid lines ("a" points) and vertical grid lines
+// ("b" points) are walked by two cursors that skip crossings outside the
+// open grid square; the a cursor runs backwards for quadrant-0 angles (the
+// reversed a list of SortIntersectionPoints) and ties go to b.
+template <class Emit>
+__device__ __forceinline__ int trace_ray(const DevGeom& G, int a, int c,
+                                         Emit&& emit) {
+  const int g = G.C;
+  const float xi = -1e6f;
+  const float yi = G.yi[c];
+  const float s = G.sinq[a], co = G.cosq[a];
+  const float srcx = fsub(fmul(xi, co), fmul(yi, s));
+  const float srcy = fadd(fmul(xi, s), fmul(yi, co));
+  const float detx = -fadd(fmul(xi, co), fmul(yi, s));
+  const float dety = fadd(fmul(-xi, s), fmul(yi, co));
+  const float slope = fdiv(fsub(srcy, dety), fsub(srcx, detx));
+  const float islope = fdiv(1.0f, slope);
+  const float lo = grid_line(G, 0), hi = grid_line(G, g);
+
+  const int da = G.quad[a] ? 1 : -1;
+  int na = G.quad[a] ? 0 : g;
+  float ax = 0.f;
+  for (; na >= 0 && na <= g; na += da) {
+    ax = fadd(fmul(islope, fsub(grid_line(G, na), srcy)), srcx);
+    if (ax > lo && ax < hi) break;
+  }
+  int nb = 0;
+  float by = 0.f;
+  for (; nb <= g; ++nb) {
+    by = fadd(fmul(slope, fsub(grid_line(G, nb), srcx)), srcy);
+    if (by > lo && by < hi) break;
+  }
+
+  int nseg = 0;
+  bool have_prev = false;
+  float px = 0.f, py = 0.f;
+  for (;;) {
+    const bool va = (na >= 0 && na <= g), vb = (nb <= g);
+    if (!va && !vb) break;
+    const bool take_a = va && (!vb || ax < grid_line(G, nb));
+    float x, y;
+    if (take_a) {
+      x = ax;
+      y = grid_line(G, na);
+      for (na += da; na >= 0 && na <= g; na += da) {
+        ax = fadd(fmul(islope, fsub(grid_line(G, na), srcy)), srcx);
+        if (ax > lo && ax < hi) break;
+      }
+    } else {
+      x = grid_line(G, nb);
+      y = by;
+      for (++nb; nb <= g; ++nb) {
+        by = fadd(fmul(slope, fsub(grid_line(G, nb), srcx)), srcy);
+        if (by > lo && by < hi) break;
+      }
+    }
+    if (have_prev) {
+      const float dx = fsub(x, px), dy = fsub(y, py);
+      // (x + px)/2. in the reference: float sum, exact halving
+      const float midx = fmul(fadd(x, px), 0.5f);
+      const float midy = fmul(fadd(y, py), 0.5f);
+      const float len2 = fadd(fmul(dx, dx), fmul(dy, dy));
+      const float len = fsqrt(len2);
+      const int ix = __float2int_rz(fadd(midx, G.mgrids));
+      const int iy = __float2int_rz(fadd(midy, G.mgrids));
+      emit(ix + iy * g, len, len2);
+      ++nseg;
+    }
+    px = x;
+    py = y;
+    have_prev = true;
+  }
+  return nseg;
+}
+
+// First detector column of the two-column window that holds every ray
+// crossing pixel (x, y) at angle a. A pixel's footprint on the detector is
+// (|sin|+|cos|) <= sqrt(2) wide, so with a 0.25-column margin for the
+// reference's float jitter at most two columns fall in the window. Built and
+// read with the same rounding, so construction and use agree bit for bit.
+__device__ __forceinline__ int window_c0(const DevGeom& G, int a, int x, int y) {
+  const float s = G.sinq[a], c = G.cosq[a];
+  const float px = fadd(fsub((float)x, G.halfg), 0.5f);
+  const float py = fadd(fsub((float)y, G.halfg), 0.5f);
+  const float t = fadd(fmul(-px, s), fmul(py, c));
+  const float hw = fmul(fadd(fabsf(s), fabsf(c)), 0.5f);
+  const float lo = fsub(fsub(fsub(t, hw), 0.25f), G.off);
+  return (int)ceilf(lo);
+}
+
+// ---- segment-length storage -------------------------------------------------
+enum LenKind { LK_F32 = 0, LK_BF16 = 1, LK_F16 = 2, LK_U16 = 3 };
+
+// 16-bit codes; `kind` is warp-uniform so the switch does not diverge.
+__device__ __forceinline__ float decode16(uint16_t v, int kind, float inv_scale) {
+  if (kind == LK_BF16) return __bfloat162float(__ushort_as_bfloat16(v));
+  if (kind == LK_F16) return __half2float(__ushort_as_half(v));
+  return (float)v * inv_scale;
+}
+__device__ __forceinline__ uint16_t encode16(float x, int kind, float scale) {
+  if (kind == LK_BF16) return __bfloat16_as_ushort(__float2bfloat16_rn(x));
+  if (kind == LK_F16) return __half_as_ushort(__float2half_rn(x));
+  float q = rintf(x * scale);
+  q = fminf(fmaxf(q, 0.f), 65535.f);
+  return (uint16_t)q;
+}
+
+// ---- k-slice vector loads ----------------------------------------------------
+template <int K>
+struct Vec {
+  float v[K];
+};
+
+template <int K>
+__device__ __forceinline__ Vec<K> load_vec(const float* p) {
+  Vec<K> r;
+  if constexpr (K == 1) {
+    r.v[0] = __ldg(p);
+  } else if constexpr (K == 2) {
+    float2 t = __ldg(reinterpret_cast<const float2*>(p));
+    r.v[0] = t.x;
+    r.v[1] = t.y;
+  } else {
+#pragma unroll
+    for (int j = 0; j < K; j += 4) {
+      float4 t = __ldg(reinterpret_cast<const float4*>(p + j));
+      r.v[j] = t.x;
+      r.v[j + 1] = t.y;
+      r.v[j + 2] = t.z;
+      r.v[j + 3] = t.w;
+    }
+  }
+  return r;
+}
+
+template <int K>
+__device__ __forceinline__ void store_vec(float* p, const Vec<K>& r) {
+  if constexpr (K == 1) {
+    p[0] = r.v[0];
+  } else if constexpr (K == 2) {
+    *reinterpret_cast<float2*>(p) = make_float2(r.v[0], r.v[1]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < K; j += 4)
+      *reinterpret_cast<float4*>(p + j) =
+          make_float4(r.v[j], r.v[j + 1], r.v[j + 2], r.v[j + 3]);
+  }
+}
+
+__device__ __forceinline__ int warp_max_i(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_max_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+}  // namespace tg

@@ -1,0 +1,91 @@
+// Kernel launchers shared between the kernel translation units and the plan
+// (host) code.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tg_device.cuh"
+#include "tg_penalty.cuh"
+
+namespace tg {
+
+// Device view of the traced system matrix of one geometry.
+struct MatrixDev {
+  // forward matrix, ray-major, one 32-ray group (32 adjacent columns of one
+  // angle) per warp; entry (group, step, lane) at roff[group] + step*32 + lane
+  const int64_t* roff;
+  const int* rcap;     // steps per group (max segment count of its rays)
+  const int* rnseg;    // [P*C] segments per ray
+  const int* ridx;     // pixel index per entry (explicit form)
+  const uint32_t* rcode;  // delta form: 8 x 4-bit steps per word per lane
+  const int64_t* rcoff;   // delta form: word offset per group
+  const int* rstart;      // delta form: [P*C] first pixel of each ray
+  const void* rlen;    // length per entry (float or 16-bit code)
+  const float* ra2;    // [P*C] sum of squared lengths (SIRT's a2)
+  // backward matrix, (angle, pixel)-major: dlen[(a*g*g + p)*2 + slot] is the
+  // length of ray (a, window_c0(a, p) + slot) through pixel p
+  const void* dlen;
+  const float* W;      // [g*g] total length through each pixel
+  int len_kind;        // LenKind
+  float scale, inv_scale;
+};
+
+// Which per-ray value the forward kernel stores.
+enum FwdOut { FWD_SIRT = 0, FWD_RATIO = 1, FWD_SIM = 2 };
+// What the backward kernel does with its per-pixel sums.
+enum BackEpi { EPI_UPDATE = 0, EPI_REPLICA = 1 };
+
+struct IterArgs {
+  DevGeom G;
+  MatrixDev M;
+  int K;              // slices per pass
+  int S;              // sinogram slices
+  int alg;            // 0..3
+  int exact;          // TG_MODE_EXACT
+  int delta_index;
+  // reconstruction slots: slot(true slice t) = t + vshift; layout
+  // [nslots/K][g*g][K]
+  int vshift;
+  int fshift;         // forward source slot of sinogram slice s = s + fshift
+  int nslots;
+  int slice_id, num_total_slices;  // APMLR top/bottom
+  PenaltyWeights pw;
+};
+
+// tg_trace.cu
+void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
+                        unsigned* maxlen_bits, cudaStream_t st);
+void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
+                       uint32_t* rcode, int* rstart, void* rlen, float* ra2,
+                       void* dlen, unsigned long long* overflow,
+                       cudaStream_t st);
+void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
+                    cudaStream_t st);
+void launch_trace_export(const DevGeom& G, const int64_t* offsets, int* idx,
+                         float* len, float* len2, cudaStream_t st);
+
+// tg_iter.cu
+void launch_forward(const IterArgs& A, const float* recon_batch,
+                    const float* sino_batch, float* out, int out_mode,
+                    cudaStream_t st);
+void launch_backward(const IterArgs& A, int batch, const float* recon_cur,
+                     float* recon_next, const float* upd, float* rep_num,
+                     int epi, cudaStream_t st);
+void launch_fg(const IterArgs& A, const float* recon, const float* W, float* F,
+               float* Gv, cudaStream_t st);
+void launch_update(const IterArgs& A, float* recon, const float* W,
+                   const float* F, const float* Gv, const float* rep_num,
+                   cudaStream_t st);
+void launch_sino_pack(const float* in, float* out, int P, int S, int C, int K,
+                      int apply_abs, cudaStream_t st);
+void launch_sino_unpack(const float* in, float* out, int P, int S, int C,
+                        int K, cudaStream_t st);
+void launch_recon_pack(const float* in, float* out, int nuser, int g2, int K,
+                       int slot0, int nslots, cudaStream_t st);
+void launch_recon_unpack(const float* in, float* out, int nuser, int g2, int K,
+                         int slot0, cudaStream_t st);
+void launch_fill(float* p, size_t n, float v, cudaStream_t st);
+void launch_replica_interleave(const float* rep_num, const float* W,
+                               float* out, int S, int g2, cudaStream_t st);
+
+}  // namespace tg

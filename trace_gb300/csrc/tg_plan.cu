@@ -1,0 +1,724 @@
+// Host side of the C ABI declared in include/trace_gb300.h: plan creation
+// (geometry tables, tracing, matrix construction), state upload/download,
+// and the per-iteration launch sequence.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/trace_gb300.h"
+#include "tg_kernels.cuh"
+
+using namespace tg;
+
+struct tg_plan {
+  tg_plan_desc d{};
+  int C = 0, P = 0, S = 0, K = 1;
+  int64_t g2 = 0, R = 0;
+  float mov = 0.f;
+  int len_kind = 0;
+  DevGeom G{};
+  MatrixDev M{};
+  PenaltyWeights pw_base{};
+  // device allocations
+  float *d_yi = nullptr, *d_sin = nullptr, *d_cos = nullptr;
+  int* d_quad = nullptr;
+  int64_t *d_roff = nullptr, *d_rcoff = nullptr;
+  int *d_rcap = nullptr, *d_rnseg = nullptr, *d_ridx = nullptr, *d_rstart = nullptr;
+  uint32_t* d_rcode = nullptr;
+  void* d_rlen = nullptr;
+  float* d_ra2 = nullptr;
+  void* d_dlen = nullptr;
+  float* d_W = nullptr;
+  unsigned* d_maxlen = nullptr;
+  unsigned long long* d_overflow = nullptr;
+  float* d_sino = nullptr;
+  float* d_recon[2] = {nullptr, nullptr};
+  int cur = 0;
+  float* d_upd = nullptr;
+  float* d_rep = nullptr;
+  float *d_F = nullptr, *d_G = nullptr;
+  float* d_stage = nullptr;
+  size_t stage_n = 0;
+  // state
+  bool have_sino = false;
+  int layout_alg = -1;  // algorithm whose layout the reconstruction uses
+  int vshift = 0, fshift = 0, nslots = 0, halo = 0;
+  int nb = 0;  // sinogram batches
+  std::vector<int> h_nseg;
+  cudaStream_t own = nullptr, st = nullptr;
+  std::string err;
+  tg_plan_info info{};
+  int64_t dev_bytes = 0;
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int fail(tg_plan* p, int code, const std::string& msg) {
+  if (p)
+    p->err = msg;
+  else
+    g_create_error = msg;
+  return code;
+}
+
+#define TG_CUDA(plan, call)                                                  \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      return fail(plan, TG_E_CUDA,                                           \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+#define TG_TRY(x)          \
+  do {                     \
+    int rc_ = (x);         \
+    if (rc_ != TG_OK) return rc_; \
+  } while (0)
+
+template <class T>
+int dalloc(tg_plan* p, T** out, size_t count, bool zero = false) {
+  void* ptr = nullptr;
+  const size_t bytes = count * sizeof(T);
+  if (bytes == 0) {
+    *out = nullptr;
+    return TG_OK;
+  }
+  cudaError_t e = cudaMalloc(&ptr, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(p, TG_E_NOMEM,
+                "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " +
+                    cudaGetErrorString(e));
+  }
+  p->allocs.push_back(ptr);
+  p->dev_bytes += (int64_t)bytes;
+  if (zero) {
+    e = cudaMemsetAsync(ptr, 0, bytes, p->st);
+    if (e != cudaSuccess) return fail(p, TG_E_CUDA, cudaGetErrorString(e));
+  }
+  *out = static_cast<T*>(ptr);
+  return TG_OK;
+}
+
+void dfree(tg_plan* p, void* ptr, size_t bytes) {
+  if (!ptr) return;
+  for (auto& a : p->allocs)
+    if (a == ptr) a = nullptr;
+  cudaFree(ptr);
+  p->dev_bytes -= (int64_t)bytes;
+}
+
+constexpr float kPI = 3.14159265358979f;  // trace_utils.h:8
+
+int quadrant_of(float t) {
+  return ((t >= 0 && t < kPI / 2) || (t >= kPI && t < 3 * kPI / 2)) ? 1 : 0;
+}
+
+int halo_of(int alg) { return alg == TG_APMLR ? 1 : 0; }
+
+bool valid_alg(int alg) { return alg >= TG_SIRT && alg <= TG_APMLR; }
+
+// Stage host data through one reusable device buffer.
+int stage(tg_plan* p, size_t n) {
+  if (p->stage_n >= n) return TG_OK;
+  dfree(p, p->d_stage, p->stage_n * sizeof(float));
+  p->d_stage = nullptr;
+  p->stage_n = 0;
+  TG_TRY(dalloc(p, &p->d_stage, n));
+  p->stage_n = n;
+  return TG_OK;
+}
+
+void fill_weights(tg_plan* p, const tg_params* prm, PenaltyWeights& w) {
+  w = p->pw_base;
+  if (!prm) return;
+  w.beta = prm->beta;
+  w.beta1 = prm->beta1;
+  w.delta = prm->delta;
+  w.delta1 = prm->delta1;
+  // APMLR weights (apmlr.cc:40-51, 90-97, 228-233; top/bottom variants with
+  // one axial neighbour, apmlr.cc:361-370): totals evaluated in double
+  // and stored as float, exactly as the reference's initialisers do.
+  const double base[3] = {4 + 4 / std::sqrt(2.0), 3 + 2 / std::sqrt(2.0),
+                          2 + 1 / std::sqrt(2.0)};
+  const float regw = prm->regw;
+  for (int r = 0; r < 3; ++r)
+    for (int ax = 0; ax < 2; ++ax) {
+      const float total = ax == 0 ? (float)(base[r] + 2 * regw)
+                                  : (float)(base[r] + regw);
+      w.apmlr[r][ax][0] = 1 / total;
+      w.apmlr[r][ax][1] = (float)(1 / std::sqrt(2.0) / total);
+      w.apmlr[r][ax][2] = regw / total;
+    }
+}
+
+IterArgs make_args(tg_plan* p, int alg, const tg_params* prm) {
+  IterArgs A{};
+  A.G = p->G;
+  A.M = p->M;
+  A.K = p->K;
+  A.S = p->S;
+  A.alg = alg;
+  A.exact = p->d.mode == TG_MODE_EXACT;
+  A.delta_index = p->d.delta_index;
+  A.vshift = p->vshift;
+  A.fshift = p->fshift;
+  A.nslots = p->nslots;
+  A.slice_id = p->d.slice_id;
+  A.num_total_slices = p->d.num_total_slices;
+  fill_weights(p, prm, A.pw);
+  return A;
+}
+
+int check_layout(tg_plan* p, int alg) {
+  if (!valid_alg(alg)) return fail(p, TG_E_ARG, "unknown algorithm");
+  if (p->layout_alg < 0)
+    return fail(p, TG_E_STATE,
+                "no reconstruction: call tg_reset_recon or tg_set_recon first");
+  if (halo_of(alg) != p->halo)
+    return fail(p, TG_E_STATE,
+                "reconstruction layout was set up for a different algorithm "
+                "family (APMLR keeps one halo slice on each side)");
+  return TG_OK;
+}
+
+int establish_layout(tg_plan* p, int alg) {
+  if (!valid_alg(alg)) return fail(p, TG_E_ARG, "unknown algorithm");
+  const int halo = halo_of(alg);
+  int vshift = 0, fshift = 0;
+  if (alg == TG_APMLR) {
+    if (p->d.apmlr_fixed_offset) {
+      vshift = p->K;  // top halo at slot K-1, forward source aligned at s + K
+      fshift = p->K;
+    } else {
+      vshift = 1;     // top halo at slot 0 = forward source of slice 0
+      fshift = 0;
+    }
+  }
+  const int need = p->S + vshift + halo;
+  const int nslots = (need + p->K - 1) / p->K * p->K;
+  if (p->layout_alg < 0 || p->nslots != nslots || p->halo != halo ||
+      p->vshift != vshift) {
+    const size_t old_n = (size_t)p->nslots * p->g2;
+    for (int b = 0; b < 2; ++b) {
+      dfree(p, p->d_recon[b], old_n * sizeof(float));
+      p->d_recon[b] = nullptr;
+    }
+    for (int b = 0; b < 2; ++b)
+      TG_TRY(dalloc(p, &p->d_recon[b], (size_t)nslots * p->g2));
+  }
+  p->halo = halo;
+  p->vshift = vshift;
+  p->fshift = fshift;
+  p->nslots = nslots;
+  p->layout_alg = alg;
+  p->cur = 0;
+  return TG_OK;
+}
+
+float* batch_ptr(tg_plan* p, float* base, int batch_slot) {
+  return base + (int64_t)(batch_slot / p->K) * p->g2 * p->K;
+}
+
+int ensure_upd(tg_plan* p) {
+  if (p->d_upd) return TG_OK;
+  return dalloc(p, &p->d_upd, (size_t)p->R * p->K);
+}
+
+}  // namespace
+
+extern "C" {
+
+int tg_abi_version(void) { return TG_ABI_VERSION; }
+
+const char* tg_last_error(const tg_plan* plan) {
+  return plan ? plan->err.c_str() : g_create_error.c_str();
+}
+
+int tg_degree_to_radian(float* theta, int n) {
+  if (!theta || n < 0) return TG_E_ARG;
+  for (int i = 0; i < n; ++i) theta[i] = theta[i] * kPI / 180.0;  // trace_utils.cc:20
+  return TG_OK;
+}
+
+int tg_plan_create(const tg_plan_desc* desc, const float* theta,
+                   const float* sin_tab, const float* cos_tab, tg_plan** out) {
+  if (!desc || !theta || !out) return fail(nullptr, TG_E_ARG, "null argument");
+  *out = nullptr;
+  const tg_plan_desc& d = *desc;
+  if (d.num_projs < 1 || d.num_slices < 1 || d.num_cols < 2)
+    return fail(nullptr, TG_E_ARG, "need num_projs >= 1, num_slices >= 1, num_cols >= 2");
+  if (d.num_cols > 32768)
+    return fail(nullptr, TG_E_ARG, "num_cols above 32768 is not supported");
+  if (!(d.slices_per_pass == 1 || d.slices_per_pass == 2 ||
+        d.slices_per_pass == 4 || d.slices_per_pass == 8))
+    return fail(nullptr, TG_E_ARG, "slices_per_pass must be 1, 2, 4 or 8");
+  if (d.len_storage < TG_LEN_F32 || d.len_storage > TG_LEN_U16)
+    return fail(nullptr, TG_E_ARG, "unknown len_storage");
+  if (d.mode != TG_MODE_EXACT && d.mode != TG_MODE_FAST)
+    return fail(nullptr, TG_E_ARG, "unknown mode");
+  if ((sin_tab == nullptr) != (cos_tab == nullptr))
+    return fail(nullptr, TG_E_ARG, "give both sin_tab and cos_tab or neither");
+
+  tg_plan* p = new (std::nothrow) tg_plan();
+  if (!p) return fail(nullptr, TG_E_NOMEM, "host allocation failed");
+  p->d = d;
+  if (p->d.num_total_slices <= 0) p->d.num_total_slices = d.num_slices;
+  p->C = d.num_cols;
+  p->P = d.num_projs;
+  p->S = d.num_slices;
+  p->K = d.slices_per_pass;
+  p->g2 = (int64_t)p->C * p->C;
+  p->R = (int64_t)p->P * p->C;
+  p->len_kind = d.len_storage;
+  p->nb = (p->S + p->K - 1) / p->K;
+
+  auto bail = [&](int rc) {
+    g_create_error = p->err;
+    tg_plan_destroy(p);
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&p->own, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    p->err = "cudaStreamCreate failed (no CUDA device?)";
+    return bail(TG_E_CUDA);
+  }
+  p->st = p->own;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, p->st);
+
+  // geometry tables (trace_data.h:96-108, sirt.cc:117-129)
+  const int C = p->C, P = p->P;
+  const float center = (d.center <= 0.) ? static_cast<float>(C) / 2. + 1. : d.center;
+  float mov = static_cast<float>(C) / 2. - center;
+  if (mov - std::ceil(mov) < 1e-6) mov += 1e-6;
+  p->mov = mov;
+  std::vector<float> yi(C), sn(P), cs(P);
+  std::vector<int> qd(P);
+  for (int c = 0; c < C; ++c) yi[c] = (1 - C) / 2. + c + mov;
+  for (int a = 0; a < P; ++a) {
+    sn[a] = sin_tab ? sin_tab[a] : sinf(theta[a]);
+    cs[a] = cos_tab ? cos_tab[a] : cosf(theta[a]);
+    qd[a] = quadrant_of(theta[a]);
+  }
+  int rc;
+  if ((rc = dalloc(p, &p->d_yi, C)) || (rc = dalloc(p, &p->d_sin, P)) ||
+      (rc = dalloc(p, &p->d_cos, P)) || (rc = dalloc(p, &p->d_quad, P)))
+    return bail(rc);
+  cudaMemcpyAsync(p->d_yi, yi.data(), C * 4, cudaMemcpyHostToDevice, p->st);
+  cudaMemcpyAsync(p->d_sin, sn.data(), P * 4, cudaMemcpyHostToDevice, p->st);
+  cudaMemcpyAsync(p->d_cos, cs.data(), P * 4, cudaMemcpyHostToDevice, p->st);
+  cudaMemcpyAsync(p->d_quad, qd.data(), P * 4, cudaMemcpyHostToDevice, p->st);
+
+  DevGeom& G = p->G;
+  G.C = C;
+  G.P = P;
+  G.gpa = (C + 31) / 32;
+  G.gpr = (C + 31) / 32;
+  G.halfg = 0.5f * (float)C;
+  G.mgrids = C / 2.;
+  G.off = (float)((1.0 - C) / 2.0 + (double)mov);
+  G.yi = p->d_yi;
+  G.sinq = p->d_sin;
+  G.cosq = p->d_cos;
+  G.quad = p->d_quad;
+
+  // pass 1: segment counts, per-group capacity, longest segment
+  const int ngroups = P * G.gpa;
+  if ((rc = dalloc(p, &p->d_rnseg, (size_t)p->R)) ||
+      (rc = dalloc(p, &p->d_rcap, (size_t)ngroups)) ||
+      (rc = dalloc(p, &p->d_maxlen, 1, true)) ||
+      (rc = dalloc(p, &p->d_overflow, 1, true)))
+    return bail(rc);
+  launch_trace_count(G, p->d_rnseg, p->d_rcap, p->d_maxlen, p->st);
+  std::vector<int> rcap(ngroups);
+  unsigned maxbits = 0;
+  p->h_nseg.resize(p->R);
+  cudaMemcpyAsync(rcap.data(), p->d_rcap, ngroups * 4, cudaMemcpyDeviceToHost, p->st);
+  cudaMemcpyAsync(&maxbits, p->d_maxlen, 4, cudaMemcpyDeviceToHost, p->st);
+  cudaMemcpyAsync(p->h_nseg.data(), p->d_rnseg, p->R * 4, cudaMemcpyDeviceToHost, p->st);
+  if (cudaStreamSynchronize(p->st) != cudaSuccess) {
+    p->err = std::string("tracing failed: ") + cudaGetErrorString(cudaGetLastError());
+    return bail(TG_E_CUDA);
+  }
+  float maxlen;
+  std::memcpy(&maxlen, &maxbits, 4);
+  int64_t nseg_total = 0;
+  for (int v : p->h_nseg) nseg_total += v;
+
+  // layout of the forward matrix: exclusive scans of the group capacities
+  std::vector<int64_t> roff(ngroups), rcoff(ngroups);
+  int64_t entries = 0, words = 0;
+  for (int i = 0; i < ngroups; ++i) {
+    roff[i] = entries;
+    rcoff[i] = words;
+    entries += (int64_t)rcap[i] * 32;
+    words += (int64_t)((rcap[i] + 7) / 8) * 32;
+  }
+  const bool l16 = p->len_kind != TG_LEN_F32;
+  const size_t lbytes = l16 ? 2 : 4;
+  if ((rc = dalloc(p, &p->d_roff, (size_t)ngroups)) ||
+      (rc = dalloc(p, &p->d_ra2, (size_t)p->R)))
+    return bail(rc);
+  cudaMemcpyAsync(p->d_roff, roff.data(), ngroups * 8, cudaMemcpyHostToDevice, p->st);
+  if (d.delta_index) {
+    if ((rc = dalloc(p, &p->d_rcoff, (size_t)ngroups)) ||
+        (rc = dalloc(p, &p->d_rcode, (size_t)words, true)) ||
+        (rc = dalloc(p, &p->d_rstart, (size_t)p->R, true)))
+      return bail(rc);
+    cudaMemcpyAsync(p->d_rcoff, rcoff.data(), ngroups * 8, cudaMemcpyHostToDevice, p->st);
+  } else {
+    if ((rc = dalloc(p, &p->d_ridx, (size_t)entries, true))) return bail(rc);
+  }
+  if (l16) {
+    uint16_t* t;
+    if ((rc = dalloc(p, &t, (size_t)entries, true))) return bail(rc);
+    p->d_rlen = t;
+  } else {
+    float* t;
+    if ((rc = dalloc(p, &t, (size_t)entries, true))) return bail(rc);
+    p->d_rlen = t;
+  }
+  const size_t dense_n = (size_t)P * p->g2 * 2;
+  if (l16) {
+    uint16_t* t;
+    if ((rc = dalloc(p, &t, dense_n, true))) return bail(rc);
+    p->d_dlen = t;
+  } else {
+    float* t;
+    if ((rc = dalloc(p, &t, dense_n, true))) return bail(rc);
+    p->d_dlen = t;
+  }
+  if ((rc = dalloc(p, &p->d_W, (size_t)p->g2))) return bail(rc);
+
+  MatrixDev& M = p->M;
+  M.roff = p->d_roff;
+  M.rcap = p->d_rcap;
+  M.rnseg = p->d_rnseg;
+  M.ridx = p->d_ridx;
+  M.rcode = p->d_rcode;
+  M.rcoff = p->d_rcoff;
+  M.rstart = p->d_rstart;
+  M.rlen = p->d_rlen;
+  M.ra2 = p->d_ra2;
+  M.dlen = p->d_dlen;
+  M.W = p->d_W;
+  M.len_kind = p->len_kind;
+  M.scale = maxlen > 0 ? 65535.f / maxlen : 1.f;
+  M.inv_scale = maxlen > 0 ? maxlen / 65535.f : 1.f;
+
+  // pass 2: fill both matrices; pass 3: total length per pixel
+  launch_trace_fill(G, M, p->d_ridx, p->d_rcode, p->d_rstart, p->d_rlen,
+                    p->d_ra2, p->d_dlen, p->d_overflow, p->st);
+  launch_weights(G, M, d.mode == TG_MODE_EXACT, p->d_W, p->st);
+  unsigned long long overflow = 0;
+  cudaMemcpyAsync(&overflow, p->d_overflow, 8, cudaMemcpyDeviceToHost, p->st);
+  cudaEventRecord(e1, p->st);
+  if (cudaStreamSynchronize(p->st) != cudaSuccess) {
+    p->err = std::string("matrix construction failed: ") +
+             cudaGetErrorString(cudaGetLastError());
+    return bail(TG_E_CUDA);
+  }
+  if (overflow) {
+    p->err = std::to_string(overflow) +
+             " segments fall outside the two-column pixel window or the "
+             "4-bit step code; geometry not supported by this layout";
+    return bail(TG_E_GEOMETRY);
+  }
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+
+  // PML weights (pml.h:22-29), double literals narrowed to float
+  PenaltyWeights& pw = p->pw_base;
+  pw.pml[0][0] = (float)0.1464466094;
+  pw.pml[0][1] = (float)0.10355339059;
+  pw.pml[1][0] = (float)0.226540919667;
+  pw.pml[1][1] = (float)0.1601886205;
+  pw.pml[2][0] = (float)0.36939806251;
+  pw.pml[2][1] = (float)0.26120387496;
+
+  tg_plan_info& I = p->info;
+  I.num_segments = nseg_total;
+  I.forward_bytes = entries * (int64_t)lbytes +
+                    (d.delta_index ? words * 4 + p->R * 4 : entries * 4);
+  I.backward_bytes = (int64_t)dense_n * (int64_t)lbytes;
+  I.max_segment_length = maxlen;
+  I.setup_ms = ms;
+  *out = p;
+  return TG_OK;
+}
+
+int tg_plan_destroy(tg_plan* p) {
+  if (!p) return TG_OK;
+  if (p->st) cudaStreamSynchronize(p->st);
+  for (void* a : p->allocs)
+    if (a) cudaFree(a);
+  if (p->own) cudaStreamDestroy(p->own);
+  delete p;
+  return TG_OK;
+}
+
+int tg_plan_get_info(const tg_plan* p, tg_plan_info* info) {
+  if (!p || !info) return TG_E_ARG;
+  *info = p->info;
+  info->device_bytes = p->dev_bytes;
+  info->batches = p->nb;
+  return TG_OK;
+}
+
+int tg_plan_set_stream(tg_plan* p, void* stream) {
+  if (!p) return TG_E_ARG;
+  p->st = stream ? static_cast<cudaStream_t>(stream) : p->own;
+  return TG_OK;
+}
+
+int tg_synchronize(tg_plan* p) {
+  if (!p) return TG_E_ARG;
+  TG_CUDA(p, cudaStreamSynchronize(p->st));
+  TG_CUDA(p, cudaGetLastError());
+  return TG_OK;
+}
+
+int tg_set_sinogram(tg_plan* p, const float* sino, int on_device,
+                    int apply_abs) {
+  if (!p || !sino) return p ? fail(p, TG_E_ARG, "null sinogram") : TG_E_ARG;
+  const size_t n = (size_t)p->P * p->S * p->C;
+  if (!p->d_sino) TG_TRY(dalloc(p, &p->d_sino, (size_t)p->nb * p->R * p->K));
+  TG_CUDA(p, cudaMemsetAsync(p->d_sino, 0,
+                             (size_t)p->nb * p->R * p->K * sizeof(float), p->st));
+  const float* src = sino;
+  if (!on_device) {
+    TG_TRY(stage(p, n));
+    TG_CUDA(p, cudaMemcpyAsync(p->d_stage, sino, n * sizeof(float),
+                               cudaMemcpyHostToDevice, p->st));
+    src = p->d_stage;
+  }
+  launch_sino_pack(src, p->d_sino, p->P, p->S, p->C, p->K, apply_abs, p->st);
+  TG_CUDA(p, cudaGetLastError());
+  p->have_sino = true;
+  return TG_OK;
+}
+
+int tg_reset_recon(tg_plan* p, int alg) {
+  if (!p) return TG_E_ARG;
+  TG_TRY(establish_layout(p, alg));
+  const float init = alg == TG_SIRT ? 0.f : 1.f;
+  for (int b = 0; b < 2; ++b)
+    launch_fill(p->d_recon[b], (size_t)p->nslots * p->g2, init, p->st);
+  TG_CUDA(p, cudaGetLastError());
+  return TG_OK;
+}
+
+int tg_set_recon(tg_plan* p, int alg, const float* recon, int on_device) {
+  if (!p || !recon) return p ? fail(p, TG_E_ARG, "null reconstruction") : TG_E_ARG;
+  TG_TRY(tg_reset_recon(p, alg));
+  const int nuser = p->S + 2 * p->halo;
+  const size_t n = (size_t)nuser * p->g2;
+  const float* src = recon;
+  if (!on_device) {
+    TG_TRY(stage(p, n));
+    TG_CUDA(p, cudaMemcpyAsync(p->d_stage, recon, n * sizeof(float),
+                               cudaMemcpyHostToDevice, p->st));
+    src = p->d_stage;
+  }
+  for (int b = 0; b < 2; ++b)
+    launch_recon_pack(src, p->d_recon[b], nuser, (int)p->g2, p->K,
+                      p->vshift - p->halo, p->nslots, p->st);
+  TG_CUDA(p, cudaGetLastError());
+  return TG_OK;
+}
+
+int tg_get_recon(tg_plan* p, int alg, float* recon, int on_device) {
+  if (!p || !recon) return p ? fail(p, TG_E_ARG, "null output") : TG_E_ARG;
+  TG_TRY(check_layout(p, alg));
+  const int nuser = p->S + 2 * p->halo;
+  const size_t n = (size_t)nuser * p->g2;
+  float* dst = recon;
+  if (!on_device) {
+    TG_TRY(stage(p, n));
+    dst = p->d_stage;
+  }
+  launch_recon_unpack(p->d_recon[p->cur], dst, nuser, (int)p->g2, p->K,
+                      p->vshift - p->halo, p->st);
+  TG_CUDA(p, cudaGetLastError());
+  if (!on_device) {
+    TG_CUDA(p, cudaMemcpyAsync(recon, p->d_stage, n * sizeof(float),
+                               cudaMemcpyDeviceToHost, p->st));
+    TG_CUDA(p, cudaStreamSynchronize(p->st));
+  }
+  return TG_OK;
+}
+
+static int run_forward(tg_plan* p, const IterArgs& A, int b, int out_mode,
+                       float* out) {
+  const float* src = batch_ptr(p, p->d_recon[p->cur], b * p->K + p->fshift);
+  launch_forward(A, src, p->d_sino + (int64_t)b * p->R * p->K, out, out_mode,
+                 p->st);
+  return TG_OK;
+}
+
+int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
+  if (!p || n_iter < 0) return p ? fail(p, TG_E_ARG, "bad n_iter") : TG_E_ARG;
+  TG_TRY(check_layout(p, alg));
+  if (!p->have_sino) return fail(p, TG_E_STATE, "no sinogram uploaded");
+  if (alg >= TG_PML && !prm) return fail(p, TG_E_ARG, "penalised algorithms need params");
+  TG_TRY(ensure_upd(p));
+  const IterArgs A = make_args(p, alg, prm);
+  const int mode = alg == TG_SIRT ? FWD_SIRT : FWD_RATIO;
+  for (int it = 0; it < n_iter; ++it) {
+    for (int b = 0; b < p->nb; ++b) {
+      run_forward(p, A, b, mode, p->d_upd);
+      launch_backward(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
+                      p->d_upd, nullptr, EPI_UPDATE, p->st);
+    }
+    p->cur ^= 1;
+  }
+  TG_CUDA(p, cudaGetLastError());
+  return TG_OK;
+}
+
+int tg_reduce(tg_plan* p, int alg, const tg_params* prm) {
+  if (!p) return TG_E_ARG;
+  TG_TRY(check_layout(p, alg));
+  if (!p->have_sino) return fail(p, TG_E_STATE, "no sinogram uploaded");
+  TG_TRY(ensure_upd(p));
+  if (!p->d_rep) TG_TRY(dalloc(p, &p->d_rep, (size_t)p->S * p->g2, true));
+  const IterArgs A = make_args(p, alg, prm);
+  const int mode = alg == TG_SIRT ? FWD_SIRT : FWD_RATIO;
+  for (int b = 0; b < p->nb; ++b) {
+    run_forward(p, A, b, mode, p->d_upd);
+    launch_backward(A, b, p->d_recon[p->cur], nullptr, p->d_upd, p->d_rep,
+                    EPI_REPLICA, p->st);
+  }
+  TG_CUDA(p, cudaGetLastError());
+  return TG_OK;
+}
+
+int tg_get_replica(tg_plan* p, int alg, float* replica, int on_device) {
+  if (!p || !replica) return p ? fail(p, TG_E_ARG, "null output") : TG_E_ARG;
+  TG_TRY(check_layout(p, alg));
+  if (!p->d_rep) return fail(p, TG_E_STATE, "no replica: call tg_reduce first");
+  const size_t n = (size_t)p->S * p->g2 * 2;
+  float* dst = replica;
+  if (!on_device) {
+    TG_TRY(stage(p, n));
+    dst = p->d_stage;
+  }
+  launch_replica_interleave(p->d_rep, p->d_W, dst, p->S, (int)p->g2, p->st);
+  TG_CUDA(p, cudaGetLastError());
+  if (!on_device) {
+    TG_CUDA(p, cudaMemcpyAsync(replica, p->d_stage, n * sizeof(float),
+                               cudaMemcpyDeviceToHost, p->st));
+    TG_CUDA(p, cudaStreamSynchronize(p->st));
+  }
+  return TG_OK;
+}
+
+int tg_reset_replica(tg_plan* p) {
+  if (!p) return TG_E_ARG;
+  if (p->d_rep)
+    TG_CUDA(p, cudaMemsetAsync(p->d_rep, 0, (size_t)p->S * p->g2 * sizeof(float), p->st));
+  return TG_OK;
+}
+
+int tg_calculate_fg(tg_plan* p, int alg, const tg_params* prm) {
+  if (!p) return TG_E_ARG;
+  TG_TRY(check_layout(p, alg));
+  if (alg < TG_PML) return fail(p, TG_E_ARG, "CalculateFG exists for PML and APMLR only");
+  if (!prm) return fail(p, TG_E_ARG, "null params");
+  if (!p->d_F) {
+    TG_TRY(dalloc(p, &p->d_F, (size_t)p->S * p->g2));
+    TG_TRY(dalloc(p, &p->d_G, (size_t)p->S * p->g2));
+  }
+  const IterArgs A = make_args(p, alg, prm);
+  launch_fg(A, p->d_recon[p->cur], p->d_W, p->d_F, p->d_G, p->st);
+  TG_CUDA(p, cudaGetLastError());
+  return TG_OK;
+}
+
+int tg_get_fg(tg_plan* p, float* F, float* G, int on_device) {
+  if (!p || !F || !G) return p ? fail(p, TG_E_ARG, "null output") : TG_E_ARG;
+  if (!p->d_F) return fail(p, TG_E_STATE, "no F/G: call tg_calculate_fg first");
+  const size_t bytes = (size_t)p->S * p->g2 * sizeof(float);
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  TG_CUDA(p, cudaMemcpyAsync(F, p->d_F, bytes, kind, p->st));
+  TG_CUDA(p, cudaMemcpyAsync(G, p->d_G, bytes, kind, p->st));
+  TG_CUDA(p, cudaStreamSynchronize(p->st));
+  return TG_OK;
+}
+
+int tg_update_recon(tg_plan* p, int alg, const tg_params* prm) {
+  if (!p) return TG_E_ARG;
+  TG_TRY(check_layout(p, alg));
+  if (!p->d_rep) return fail(p, TG_E_STATE, "no replica: call tg_reduce first");
+  if (alg >= TG_PML && !p->d_F)
+    return fail(p, TG_E_STATE, "call tg_calculate_fg before tg_update_recon");
+  const IterArgs A = make_args(p, alg, prm);
+  float* cur = p->d_recon[p->cur];
+  launch_update(A, cur, p->d_W, p->d_F, p->d_G, p->d_rep, p->st);
+  // keep the other buffer's copy identical so fused and operator calls mix
+  TG_CUDA(p, cudaMemcpyAsync(p->d_recon[p->cur ^ 1], cur,
+                             (size_t)p->nslots * p->g2 * sizeof(float),
+                             cudaMemcpyDeviceToDevice, p->st));
+  TG_CUDA(p, cudaGetLastError());
+  return TG_OK;
+}
+
+int tg_forward_project(tg_plan* p, int alg, const tg_params* prm, float* sim,
+                       int on_device) {
+  if (!p || !sim) return p ? fail(p, TG_E_ARG, "null output") : TG_E_ARG;
+  TG_TRY(check_layout(p, alg));
+  const size_t packed = (size_t)p->nb * p->R * p->K;
+  const size_t n = (size_t)p->P * p->S * p->C;
+  TG_TRY(stage(p, packed + (on_device ? 0 : n)));
+  const IterArgs A = make_args(p, alg, prm);
+  for (int b = 0; b < p->nb; ++b)
+    run_forward(p, A, b, FWD_SIM, p->d_stage + (int64_t)b * p->R * p->K);
+  float* dst = on_device ? sim : p->d_stage + packed;
+  launch_sino_unpack(p->d_stage, dst, p->P, p->S, p->C, p->K, p->st);
+  TG_CUDA(p, cudaGetLastError());
+  if (!on_device)
+    TG_CUDA(p, cudaMemcpyAsync(sim, dst, n * sizeof(float), cudaMemcpyDeviceToHost, p->st));
+  TG_CUDA(p, cudaStreamSynchronize(p->st));
+  return TG_OK;
+}
+
+int tg_trace_rays(tg_plan* p, int32_t* counts, const int64_t* offsets,
+                  int32_t* idx, float* len, float* len2) {
+  if (!p || !counts) return p ? fail(p, TG_E_ARG, "null counts") : TG_E_ARG;
+  std::memcpy(counts, p->h_nseg.data(), p->R * sizeof(int32_t));
+  if (!idx) return TG_OK;
+  if (!offsets || !len) return fail(p, TG_E_ARG, "offsets and len are required with idx");
+  const int64_t total = offsets[p->R];
+  int64_t* d_off = nullptr;
+  int* d_idx = nullptr;
+  float *d_len = nullptr, *d_len2 = nullptr;
+  int rc;
+  if ((rc = dalloc(p, &d_off, (size_t)p->R + 1)) || (rc = dalloc(p, &d_idx, (size_t)total)) ||
+      (rc = dalloc(p, &d_len, (size_t)total)) ||
+      (len2 && (rc = dalloc(p, &d_len2, (size_t)total))))
+    return rc;
+  TG_CUDA(p, cudaMemcpyAsync(d_off, offsets, (p->R + 1) * 8, cudaMemcpyHostToDevice, p->st));
+  launch_trace_export(p->G, d_off, d_idx, d_len, d_len2, p->st);
+  TG_CUDA(p, cudaMemcpyAsync(idx, d_idx, total * 4, cudaMemcpyDeviceToHost, p->st));
+  TG_CUDA(p, cudaMemcpyAsync(len, d_len, total * 4, cudaMemcpyDeviceToHost, p->st));
+  if (len2) TG_CUDA(p, cudaMemcpyAsync(len2, d_len2, total * 4, cudaMemcpyDeviceToHost, p->st));
+  TG_CUDA(p, cudaStreamSynchronize(p->st));
+  dfree(p, d_off, (p->R + 1) * 8);
+  dfree(p, d_idx, total * 4);
+  dfree(p, d_len, total * 4);
+  dfree(p, d_len2, len2 ? total * 4 : 0);
+  return TG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,215 @@
+// Tracing kernels: one thread per ray, one warp per 32 adjacent detector
+// columns of one angle. They build, once per geometry, the two device forms
+// of the system matrix the iterations stream:
+//   * forward (ray-major): each ray's segments in the reference's order,
+//     stored step-interleaved across the 32 rays of a warp so that every
+//     load of the forward projection is one coalesced 128-byte row;
+//   * backward (angle, pixel)-major: for every pixel and angle the lengths of
+//     the (at most two) rays crossing it, in column order.
+// The tracer itself (tg::trace_ray) reproduces src/common/trace_utils.cc:48-216.
+#include "tg_kernels.cuh"
+
+namespace tg {
+
+namespace {
+
+constexpr int kTraceBlock = 128;
+
+__global__ void __launch_bounds__(kTraceBlock)
+    k_trace_count(DevGeom G, int ngroups, int* nseg, int* rcap,
+                  unsigned* maxlen_bits) {
+  const int grp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (grp >= ngroups) return;  // warp-uniform
+  const int a = grp / G.gpa;
+  const int c = (grp - a * G.gpa) * 32 + lane;
+  int n = 0;
+  float ml = 0.f;
+  if (c < G.C) {
+    n = trace_ray(G, a, c, [&](int, float l, float) { ml = fmaxf(ml, l); });
+    nseg[(int64_t)a * G.C + c] = n;
+  }
+  const int cap = warp_max_i(n);
+  const float m = warp_max_f(ml);
+  if (lane == 0) {
+    rcap[grp] = cap;
+    atomicMax(maxlen_bits, __float_as_uint(m));  // lengths are >= 0
+  }
+}
+
+template <bool L16, bool DELTA>
+__global__ void __launch_bounds__(kTraceBlock)
+    k_trace_fill(DevGeom G, MatrixDev M, int ngroups, int* ridx,
+                 uint32_t* rcode, int* rstart, void* rlen, float* ra2,
+                 void* dlen, unsigned long long* overflow) {
+  const int grp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (grp >= ngroups) return;
+  const int a = grp / G.gpa;
+  const int c = (grp - a * G.gpa) * 32 + lane;
+  if (c >= G.C) return;
+  const int g = G.C;
+  const int64_t g2 = (int64_t)g * g;
+  const int64_t r = (int64_t)a * G.C + c;
+  const int64_t base = M.roff[grp] + lane;
+  const int64_t cbase = DELTA ? M.rcoff[grp] + lane : 0;
+  float a2 = 0.f;
+  int s = 0, pix = 0, piy = 0;
+  uint32_t word = 0;
+  unsigned long long bad = 0;
+  trace_ray(G, a, c, [&](int idx, float l, float l2) {
+    const int64_t e = base + (int64_t)s * 32;
+    const int ix = idx % g, iy = idx / g;
+    if (DELTA) {
+      if (s == 0) {
+        rstart[r] = idx;
+      } else {
+        const int dx = ix - pix, dy = iy - piy;
+        if (dx < 0 || dx > 1 || dy < -1 || dy > 1) ++bad;
+        word |= (uint32_t)(dx | ((dy + 1) << 1)) << (4 * (s & 7));
+      }
+      if ((s & 7) == 7) {
+        rcode[cbase + (int64_t)(s >> 3) * 32] = word;
+        word = 0;
+      }
+    } else {
+      ridx[e] = idx;
+    }
+    pix = ix;
+    piy = iy;
+    if (L16)
+      reinterpret_cast<uint16_t*>(rlen)[e] = encode16(l, M.len_kind, M.scale);
+    else
+      reinterpret_cast<float*>(rlen)[e] = l;
+    a2 = fadd(a2, l2);
+    // backward matrix: slot = column offset inside the pixel's window
+    const int slot = c - window_c0(G, a, ix, iy);
+    if (slot < 0 || slot > 1) {
+      ++bad;
+    } else {
+      // A present entry never stores +0: a zero length is kept as -0 so the
+      // backprojection still visits it (0 * a non-finite factor is NaN in
+      // the reference too). The 16-bit fixed-point code has no -0.
+      const int64_t pos = ((int64_t)a * g2 + idx) * 2 + slot;
+      if (L16) {
+        uint16_t* d = reinterpret_cast<uint16_t*>(dlen);
+        const float cur = decode16(d[pos], M.len_kind, M.inv_scale);
+        uint16_t code = encode16(cur + l, M.len_kind, M.scale);
+        if (code == 0 && M.len_kind != LK_U16) code = 0x8000u;
+        d[pos] = code;
+      } else {
+        float* d = reinterpret_cast<float*>(dlen);
+        const float nv = fadd(d[pos], l);
+        d[pos] = (__float_as_uint(nv) == 0u) ? -0.0f : nv;
+      }
+    }
+    ++s;
+  });
+  if (DELTA && (s & 7) != 0 && s > 0)
+    rcode[cbase + (int64_t)(s >> 3) * 32] = word;
+  ra2[r] = a2;
+  if (bad) atomicAdd(overflow, bad);
+}
+
+// Total length through each pixel: the reference's replica[2p+1]
+// (sirt.cc:59), identical for every slice, so computed once.
+template <bool L16>
+__global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W) {
+  const int g = G.C;
+  const int64_t g2 = (int64_t)g * g;
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g2) return;
+  float sum = 0.f, comp = 0.f;
+  for (int a = 0; a < G.P; ++a) {
+    const int64_t pos = ((int64_t)a * g2 + p) * 2;
+    float l0, l1;
+    if (L16) {
+      const uint32_t w =
+          reinterpret_cast<const uint32_t*>(M.dlen)[pos >> 1];
+      l0 = decode16((uint16_t)(w & 0xffffu), M.len_kind, M.inv_scale);
+      l1 = decode16((uint16_t)(w >> 16), M.len_kind, M.inv_scale);
+    } else {
+      const float2 v = reinterpret_cast<const float2*>(M.dlen)[pos >> 1];
+      l0 = v.x;
+      l1 = v.y;
+    }
+    if (exact) {
+      sum = fadd(fadd(sum, l0), l1);
+    } else {
+      float y = l0 - comp, t = sum + y;
+      comp = (t - sum) - y;
+      sum = t;
+      y = l1 - comp;
+      t = sum + y;
+      comp = (t - sum) - y;
+      sum = t;
+    }
+  }
+  W[p] = sum;
+}
+
+__global__ void __launch_bounds__(kTraceBlock)
+    k_trace_export(DevGeom G, int nrays, const int64_t* offsets, int* idx,
+                   float* len, float* len2) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrays) return;
+  const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
+  int64_t o = offsets[r];
+  trace_ray(G, a, c, [&](int i, float l, float l2) {
+    idx[o] = i;
+    len[o] = l;
+    if (len2) len2[o] = l2;
+    ++o;
+  });
+}
+
+}  // namespace
+
+void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
+                        unsigned* maxlen_bits, cudaStream_t st) {
+  const int ngroups = G.P * G.gpa;
+  const int blocks = (ngroups * 32 + kTraceBlock - 1) / kTraceBlock;
+  k_trace_count<<<blocks, kTraceBlock, 0, st>>>(G, ngroups, nseg, rcap,
+                                                 maxlen_bits);
+}
+
+void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
+                       uint32_t* rcode, int* rstart, void* rlen, float* ra2,
+                       void* dlen, unsigned long long* overflow,
+                       cudaStream_t st) {
+  const int ngroups = G.P * G.gpa;
+  const int blocks = (ngroups * 32 + kTraceBlock - 1) / kTraceBlock;
+  const bool l16 = M.len_kind != LK_F32;
+  const bool delta = rcode != nullptr;
+  if (l16 && delta)
+    k_trace_fill<true, true><<<blocks, kTraceBlock, 0, st>>>(
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, dlen, overflow);
+  else if (l16)
+    k_trace_fill<true, false><<<blocks, kTraceBlock, 0, st>>>(
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, dlen, overflow);
+  else if (delta)
+    k_trace_fill<false, true><<<blocks, kTraceBlock, 0, st>>>(
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, dlen, overflow);
+  else
+    k_trace_fill<false, false><<<blocks, kTraceBlock, 0, st>>>(
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, dlen, overflow);
+}
+
+void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
+                    cudaStream_t st) {
+  const int64_t g2 = (int64_t)G.C * G.C;
+  const int blocks = (int)((g2 + 255) / 256);
+  if (M.len_kind != LK_F32)
+    k_weights<true><<<blocks, 256, 0, st>>>(G, M, exact, W);
+  else
+    k_weights<false><<<blocks, 256, 0, st>>>(G, M, exact, W);
+}
+
+void launch_trace_export(const DevGeom& G, const int64_t* offsets, int* idx,
+                         float* len, float* len2, cudaStream_t st) {
+  const int nrays = G.P * G.C;
+  k_trace_export<<<(nrays + kTraceBlock - 1) / kTraceBlock, kTraceBlock, 0,
+                   st>>>(G, nrays, offsets, idx, len, len2);
+}
+
+}  // namespace tg
