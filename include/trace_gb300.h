@@ -111,6 +111,13 @@ typedef struct {
   int batches;                /* ceil(stored slices / slices_per_pass) */
 } tg_plan_info;
 
+typedef struct {
+  double forward_ms;          /* summed device time of forward launches */
+  double backward_ms;         /* backprojection (+ fused update) launches */
+  double other_ms;            /* operator-level penalty/update launches */
+  int64_t forward_launches, backward_launches, other_launches;
+} tg_timing;
+
 typedef struct tg_plan tg_plan;
 
 int tg_abi_version(void);
@@ -128,6 +135,13 @@ int tg_plan_get_info(const tg_plan* plan, tg_plan_info* info);
 int tg_plan_set_stream(tg_plan* plan, void* stream);
 int tg_synchronize(tg_plan* plan);
 const char* tg_last_error(const tg_plan* plan);
+
+/* Per-kernel device timers (CUDA events around each launch on the plan's
+ * stream), the counterpart of the reference drivers' -DTIMERON phase timers
+ * (sirt_main.cc:174-223). tg_plan_set_timing(plan, 1) clears and starts;
+ * tg_plan_get_timing synchronizes the stream and returns the sums. */
+int tg_plan_set_timing(tg_plan* plan, int enable);
+int tg_plan_get_timing(tg_plan* plan, tg_timing* out);
 
 /* In-place degrees -> radians with the reference's float constant. Host. */
 int tg_degree_to_radian(float* theta, int n);

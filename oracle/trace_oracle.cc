@@ -22,6 +22,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -74,11 +75,26 @@ void make_geometry(Geometry& G, int C, int P, float center, const float* theta,
 }
 
 // One traced segment: pixel index, float length and squared length, and
-// the double-precision length of the same (float) crossing points.
+// (when requested) the double-precision length of the same float points.
 struct Seg {
   int idx;
   float len, len2;
   double dlen, dlen2;
+};
+
+// Per-thread scratch of the tracer: the crossing coordinates of one ray
+// with every horizontal (cx) and vertical (cy) grid line.
+struct TraceWs {
+  std::vector<float> cx, cy;
+  std::vector<Seg> segs;
+  // merged crossing points and per-segment results of trace_ray_arrays
+  std::vector<float> px, py, len, len2;
+  std::vector<int> idx;
+  explicit TraceWs(int g)
+      : cx(g + 1), cy(g + 1), px(2 * g + 2), py(2 * g + 2), len(2 * g + 2),
+        len2(2 * g + 2), idx(2 * g + 2) {
+    segs.reserve(2 * g + 2);
+  }
 };
 
 // Streams the segments of ray (p, c) to `emit` in the reference's order.
@@ -90,8 +106,8 @@ struct Seg {
 // quadrant 0) with the b list by x, taking b on ties. Here the two lists
 // are walked by cursors that skip rejected crossings, so each output point
 // is produced in the same order without the arrays.
-template <class Emit>
-int trace_ray(const Geometry& G, int p, int c, Emit&& emit) {
+template <bool WANT_DOUBLE = false, class Emit>
+int trace_ray(const Geometry& G, int p, int c, TraceWs& ws, Emit&& emit) {
   const int g = G.C;
   const float* grid = G.grid.data();
   const float xi = -1e6f;
@@ -104,13 +120,20 @@ int trace_ray(const Geometry& G, int p, int c, Emit&& emit) {
   const float slope = (srcy - dety) / (srcx - detx);
   const float islope = 1 / slope;
   const float lo = grid[0], hi = grid[g];
+  // all crossings first (a vectorisable loop, as CalculateCoordinates)
+  float* cx = ws.cx.data();
+  float* cy = ws.cy.data();
+  for (int n = 0; n <= g; ++n) {
+    cx[n] = islope * (grid[n] - srcy) + srcx;
+    cy[n] = slope * (grid[n] - srcx) + srcy;
+  }
 
   const int da = G.quad[p] ? 1 : -1;
   int na = G.quad[p] ? 0 : g;
   float ax = 0.f;
   auto seek_a = [&]() {
     for (; na >= 0 && na <= g; na += da) {
-      ax = islope * (grid[na] - srcy) + srcx;
+      ax = cx[na];
       if (ax > lo && ax < hi) return;
     }
   };
@@ -118,7 +141,7 @@ int trace_ray(const Geometry& G, int p, int c, Emit&& emit) {
   float by = 0.f;
   auto seek_b = [&]() {
     for (; nb <= g; ++nb) {
-      by = slope * (grid[nb] - srcx) + srcy;
+      by = cy[nb];
       if (by > lo && by < hi) return;
     }
   };
@@ -153,15 +176,76 @@ int trace_ray(const Geometry& G, int p, int c, Emit&& emit) {
       const int ix = midx + G.mgrids;  // truncation, as trace_utils.cc:179
       const int iy = midy + G.mgrids;
       sg.idx = ix + iy * g;
-      const double ddx = (double)x - (double)px, ddy = (double)y - (double)py;
-      sg.dlen2 = ddx * ddx + ddy * ddy;
-      sg.dlen = std::sqrt(sg.dlen2);
+      if (WANT_DOUBLE) {
+        const double ddx = (double)x - (double)px, ddy = (double)y - (double)py;
+        sg.dlen2 = ddx * ddx + ddy * ddy;
+        sg.dlen = std::sqrt(sg.dlen2);
+      }
       emit(sg);
       ++nseg;
     }
     px = x;
     py = y;
     have_prev = true;
+  }
+  return nseg;
+}
+
+// The same tracing as trace_ray in three passes over arrays (crossings,
+// merge, lengths), so the first and last passes vectorise. Fills ws.idx,
+// ws.len, ws.len2 and returns the segment count.
+int trace_ray_arrays(const Geometry& G, int p, int c, TraceWs& ws) {
+  const int g = G.C;
+  const float* grid = G.grid.data();
+  const float xi = -1e6f;
+  const float yi = G.yi[c];
+  const float s = G.sinq[p], co = G.cosq[p];
+  const float srcx = xi * co - yi * s;
+  const float srcy = xi * s + yi * co;
+  const float detx = -1 * (xi * co + yi * s);
+  const float dety = -xi * s + yi * co;
+  const float slope = (srcy - dety) / (srcx - detx);
+  const float islope = 1 / slope;
+  const float lo = grid[0], hi = grid[g];
+  float* cx = ws.cx.data();
+  float* cy = ws.cy.data();
+  for (int n = 0; n <= g; ++n) {
+    cx[n] = islope * (grid[n] - srcy) + srcx;
+    cy[n] = slope * (grid[n] - srcx) + srcy;
+  }
+  float* px = ws.px.data();
+  float* py = ws.py.data();
+  const int da = G.quad[p] ? 1 : -1;
+  int na = G.quad[p] ? 0 : g, nb = 0, m = 0;
+  while (na >= 0 && na <= g && !(cx[na] > lo && cx[na] < hi)) na += da;
+  while (nb <= g && !(cy[nb] > lo && cy[nb] < hi)) ++nb;
+  for (;;) {
+    const bool va = (na >= 0 && na <= g), vb = (nb <= g);
+    if (!va && !vb) break;
+    if (va && (!vb || cx[na] < grid[nb])) {
+      px[m] = cx[na];
+      py[m] = grid[na];
+      for (na += da; na >= 0 && na <= g && !(cx[na] > lo && cx[na] < hi); na += da) {
+      }
+    } else {
+      px[m] = grid[nb];
+      py[m] = cy[nb];
+      for (++nb; nb <= g && !(cy[nb] > lo && cy[nb] < hi); ++nb) {
+      }
+    }
+    ++m;
+  }
+  const int nseg = m > 1 ? m - 1 : 0;
+  float* ln = ws.len.data();
+  float* ln2 = ws.len2.data();
+  int* ix = ws.idx.data();
+  const float mg = G.mgrids;
+  for (int i = 0; i < nseg; ++i) {
+    const float dx = px[i + 1] - px[i], dy = py[i + 1] - py[i];
+    const float midx = (px[i + 1] + px[i]) / 2., midy = (py[i + 1] + py[i]) / 2.;
+    ln2[i] = dx * dx + dy * dy;
+    ln[i] = std::sqrt(ln2[i]);
+    ix[i] = (int)(midx + mg) + (int)(midy + mg) * g;
   }
   return nseg;
 }
@@ -280,16 +364,57 @@ struct Run {
     return recon.data() + (size_t)off * g2;
   }
 
+  // Float path of one ray, over the tracer's arrays (the reference's loops:
+  // CalculateSimdata then UpdateReconReplica).
+  void reduce_ray_f32(int p, int c, const T* rc, T* row, float rayv,
+                      TraceWs& ws) {
+    const int n = trace_ray_arrays(G, p, c, ws);
+    const int* ix = ws.idx.data();
+    const float* ln = ws.len.data();
+    float sim = 0.f;
+    for (int i = 0; i < n; ++i) sim += (float)rc[ix[i]] * ln[i];
+    if (A.alg == TOR_SIRT) {
+      float a2 = 0.f;
+      const float* ln2 = ws.len2.data();
+      for (int i = 0; i < n; ++i) a2 += ln2[i];
+      const float upd = (rayv - sim) / a2;
+      for (int i = 0; i < n; ++i) {
+        row[(size_t)ix[i] * 2] += ln[i] * upd;
+        row[(size_t)ix[i] * 2 + 1] += ln[i];
+      }
+    } else if (A.alg == TOR_MLEM) {
+      const float upd = rayv / sim;
+      for (int i = 0; i < n; ++i) {
+        row[(size_t)ix[i] * 2] += ln[i] * upd;
+        row[(size_t)ix[i] * 2 + 1] += ln[i];
+      }
+    } else {
+      const float upd = rayv / sim;
+      for (int i = 0; i < n; ++i) {
+        row[(size_t)ix[i] * 2] -= rc[ix[i]] * ln[i] * upd;
+        row[(size_t)ix[i] * 2 + 1] += ln[i];
+      }
+    }
+  }
+
   // One work unit = one (projection, slice) row of C rays, exactly the
   // chunk the reference engine hands out (sirt_main.cc:172).
-  void reduce_unit(long u, std::vector<T>& rep, std::vector<Seg>& buf) {
+  void reduce_unit(long u, std::vector<T>& rep, TraceWs& ws) {
+    std::vector<Seg>& buf = ws.segs;
     const int p = (int)(u / S), s = (int)(u % S);
     const T* rc = fwd_slice(s);
     T* row = rep.data() + (size_t)s * 2 * g2;
     const float* rays = sino.data() + ((size_t)p * S + s) * g;
     for (int c = 0; c < g; ++c) {
+      if (A.precision == TOR_F32) {
+        reduce_ray_f32(p, c, rc, row, rays[c], ws);
+        continue;
+      }
       buf.clear();
-      trace_ray(G, p, c, [&](const Seg& sg) { buf.push_back(sg); });
+      if (A.dlen)
+        trace_ray<true>(G, p, c, ws, [&](const Seg& sg) { buf.push_back(sg); });
+      else
+        trace_ray<false>(G, p, c, ws, [&](const Seg& sg) { buf.push_back(sg); });
       T sim = 0.;
       for (const Seg& sg : buf) sim += rc[sg.idx] * seg_len(sg);
       const T ray = rays[c];
@@ -417,13 +542,14 @@ struct Run {
     const int nthr = T_ < 1 ? 1 : T_;
     const size_t rep_n = (size_t)S * 2 * g2;
     std::vector<std::vector<T>> reps(nthr, std::vector<T>(rep_n, (T)0.));
-    std::vector<std::vector<Seg>> bufs(nthr);
-    for (auto& b : bufs) b.reserve(2 * g + 2);
+    // one heap-allocated workspace per thread (no shared cache lines)
+    std::vector<std::unique_ptr<TraceWs>> wss;
+    for (int t = 0; t < nthr; ++t) wss.emplace_back(new TraceWs(g));
     const long units = (long)A.num_projs * S;
     auto t0 = std::chrono::steady_clock::now();
     for (int it = 0; it < A.n_iter; ++it) {
       parallel_for(units, nthr,
-                   [&](long u, int t) { reduce_unit(u, reps[t], bufs[t]); });
+                   [&](long u, int t) { reduce_unit(u, reps[t], *wss[t]); });
       // pairwise tree combination, as ParInPlaceLocalSynch(…, 2, …)
       for (int step = 1; step < nthr; step *= 2)
         parallel_for((nthr + 2 * step - 1) / (2 * step), nthr, [&](long i, int) {
@@ -478,8 +604,9 @@ int tor_trace_counts(int num_cols, int num_projs, float center,
   Geometry G;
   make_geometry(G, num_cols, num_projs, center, nullptr, sinq, cosq, quad);
   parallel_for((long)num_projs, threads, [&](long p, int) {
+    TraceWs ws(num_cols);
     for (int c = 0; c < num_cols; ++c)
-      counts[p * num_cols + c] = trace_ray(G, (int)p, c, [](const Seg&) {});
+      counts[p * num_cols + c] = trace_ray(G, (int)p, c, ws, [](const Seg&) {});
   });
   return 0;
 }
@@ -492,9 +619,10 @@ int tor_trace_fill(int num_cols, int num_projs, float center, const float* sinq,
   Geometry G;
   make_geometry(G, num_cols, num_projs, center, nullptr, sinq, cosq, quad);
   parallel_for((long)num_projs, threads, [&](long p, int) {
+    TraceWs ws(num_cols);
     for (int c = 0; c < num_cols; ++c) {
       int64_t o = offsets[p * num_cols + c];
-      trace_ray(G, (int)p, c, [&](const Seg& s) {
+      trace_ray(G, (int)p, c, ws, [&](const Seg& s) {
         idx[o] = s.idx;
         len[o] = s.len;
         if (len2) len2[o] = s.len2;
@@ -521,10 +649,11 @@ int tor_forward(int num_cols, int num_projs, int num_slices, float center,
   make_geometry(G, num_cols, num_projs, center, nullptr, sinq, cosq, quad);
   const size_t g2 = (size_t)num_cols * num_cols;
   parallel_for((long)num_projs, threads, [&](long p, int) {
-    std::vector<Seg> buf;
+    TraceWs ws(num_cols);
+    std::vector<Seg>& buf = ws.segs;
     for (int c = 0; c < num_cols; ++c) {
       buf.clear();
-      trace_ray(G, (int)p, c, [&](const Seg& sg) { buf.push_back(sg); });
+      trace_ray(G, (int)p, c, ws, [&](const Seg& sg) { buf.push_back(sg); });
       for (int s = 0; s < num_slices; ++s) {
         const float* rc = recon + (size_t)s * g2;
         float acc = 0.f;

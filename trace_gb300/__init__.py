@@ -33,7 +33,8 @@ EXPORTED = [
     "tg_degree_to_radian", "tg_set_sinogram", "tg_reset_recon", "tg_set_recon",
     "tg_get_recon", "tg_reduce", "tg_get_replica", "tg_calculate_fg",
     "tg_get_fg", "tg_update_recon", "tg_reset_replica", "tg_iterate",
-    "tg_forward_project", "tg_trace_rays",
+    "tg_forward_project", "tg_trace_rays", "tg_plan_set_timing",
+    "tg_plan_get_timing",
 ]
 
 
@@ -62,6 +63,12 @@ class PlanInfo(C.Structure):
                 ("backward_bytes", C.c_int64), ("device_bytes", C.c_int64),
                 ("max_segment_length", C.c_float), ("setup_ms", C.c_double),
                 ("batches", C.c_int)]
+
+
+class Timing(C.Structure):
+    _fields_ = [("forward_ms", C.c_double), ("backward_ms", C.c_double),
+                ("other_ms", C.c_double), ("forward_launches", C.c_int64),
+                ("backward_launches", C.c_int64), ("other_launches", C.c_int64)]
 
 
 _lib = None
@@ -171,6 +178,14 @@ class Plan:
 
     def set_stream(self, stream_ptr):
         self._chk(self._lib.tg_plan_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    def set_timing(self, enable=True):
+        self._chk(self._lib.tg_plan_set_timing(self._h, int(bool(enable))))
+
+    def timing(self) -> dict:
+        t = Timing()
+        self._chk(self._lib.tg_plan_get_timing(self._h, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in Timing._fields_}
 
     def synchronize(self):
         self._chk(self._lib.tg_synchronize(self._h))

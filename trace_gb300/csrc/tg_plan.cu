@@ -53,6 +53,10 @@ struct tg_plan {
   tg_plan_info info{};
   int64_t dev_bytes = 0;
   std::vector<void*> allocs;
+  // per-kernel timers: event pairs recorded around launches while enabled
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_used;
 };
 
 namespace {
@@ -221,6 +225,34 @@ int establish_layout(tg_plan* p, int alg) {
   p->cur = 0;
   return TG_OK;
 }
+
+// Timer bracket around one launch; kind 0 forward, 1 backward, 2 other.
+struct Timed {
+  tg_plan* p;
+  int kind;
+  cudaEvent_t b = nullptr, e = nullptr;
+  cudaEvent_t take() {
+    if (!p->ev_pool.empty()) {
+      cudaEvent_t ev = p->ev_pool.back();
+      p->ev_pool.pop_back();
+      return ev;
+    }
+    cudaEvent_t ev;
+    cudaEventCreate(&ev);
+    return ev;
+  }
+  Timed(tg_plan* pl, int k) : p(pl), kind(k) {
+    if (!p->timing) return;
+    b = take();
+    e = take();
+    cudaEventRecord(b, p->st);
+  }
+  ~Timed() {
+    if (!p->timing) return;
+    cudaEventRecord(e, p->st);
+    p->ev_used.push_back({kind, {b, e}});
+  }
+};
 
 float* batch_ptr(tg_plan* p, float* base, int batch_slot) {
   return base + (int64_t)(batch_slot / p->K) * p->g2 * p->K;
@@ -458,9 +490,47 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   return TG_OK;
 }
 
+int tg_plan_set_timing(tg_plan* p, int enable) {
+  if (!p) return TG_E_ARG;
+  if (p->st) cudaStreamSynchronize(p->st);
+  for (auto& u : p->ev_used) {
+    p->ev_pool.push_back(u.second.first);
+    p->ev_pool.push_back(u.second.second);
+  }
+  p->ev_used.clear();
+  p->timing = enable != 0;
+  return TG_OK;
+}
+
+int tg_plan_get_timing(tg_plan* p, tg_timing* out) {
+  if (!p || !out) return TG_E_ARG;
+  TG_CUDA(p, cudaStreamSynchronize(p->st));
+  std::memset(out, 0, sizeof(*out));
+  for (auto& u : p->ev_used) {
+    float ms = 0.f;
+    TG_CUDA(p, cudaEventElapsedTime(&ms, u.second.first, u.second.second));
+    if (u.first == 0) {
+      out->forward_ms += ms;
+      out->forward_launches++;
+    } else if (u.first == 1) {
+      out->backward_ms += ms;
+      out->backward_launches++;
+    } else {
+      out->other_ms += ms;
+      out->other_launches++;
+    }
+  }
+  return TG_OK;
+}
+
 int tg_plan_destroy(tg_plan* p) {
   if (!p) return TG_OK;
   if (p->st) cudaStreamSynchronize(p->st);
+  for (auto& u : p->ev_used) {
+    cudaEventDestroy(u.second.first);
+    cudaEventDestroy(u.second.second);
+  }
+  for (auto ev : p->ev_pool) cudaEventDestroy(ev);
   for (void* a : p->allocs)
     if (a) cudaFree(a);
   if (p->own) cudaStreamDestroy(p->own);
@@ -562,6 +632,7 @@ int tg_get_recon(tg_plan* p, int alg, float* recon, int on_device) {
 static int run_forward(tg_plan* p, const IterArgs& A, int b, int out_mode,
                        float* out) {
   const float* src = batch_ptr(p, p->d_recon[p->cur], b * p->K + p->fshift);
+  Timed t(p, 0);
   launch_forward(A, src, p->d_sino + (int64_t)b * p->R * p->K, out, out_mode,
                  p->st);
   return TG_OK;
@@ -578,6 +649,7 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
   for (int it = 0; it < n_iter; ++it) {
     for (int b = 0; b < p->nb; ++b) {
       run_forward(p, A, b, mode, p->d_upd);
+      Timed t(p, 1);
       launch_backward(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
                       p->d_upd, nullptr, EPI_UPDATE, p->st);
     }
@@ -597,6 +669,7 @@ int tg_reduce(tg_plan* p, int alg, const tg_params* prm) {
   const int mode = alg == TG_SIRT ? FWD_SIRT : FWD_RATIO;
   for (int b = 0; b < p->nb; ++b) {
     run_forward(p, A, b, mode, p->d_upd);
+    Timed t(p, 1);
     launch_backward(A, b, p->d_recon[p->cur], nullptr, p->d_upd, p->d_rep,
                     EPI_REPLICA, p->st);
   }
@@ -641,6 +714,7 @@ int tg_calculate_fg(tg_plan* p, int alg, const tg_params* prm) {
     TG_TRY(dalloc(p, &p->d_G, (size_t)p->S * p->g2));
   }
   const IterArgs A = make_args(p, alg, prm);
+  Timed t(p, 2);
   launch_fg(A, p->d_recon[p->cur], p->d_W, p->d_F, p->d_G, p->st);
   TG_CUDA(p, cudaGetLastError());
   return TG_OK;
@@ -665,6 +739,7 @@ int tg_update_recon(tg_plan* p, int alg, const tg_params* prm) {
     return fail(p, TG_E_STATE, "call tg_calculate_fg before tg_update_recon");
   const IterArgs A = make_args(p, alg, prm);
   float* cur = p->d_recon[p->cur];
+  Timed t(p, 2);
   launch_update(A, cur, p->d_W, p->d_F, p->d_G, p->d_rep, p->st);
   // keep the other buffer's copy identical so fused and operator calls mix
   TG_CUDA(p, cudaMemcpyAsync(p->d_recon[p->cur ^ 1], cur,
