@@ -118,22 +118,35 @@ __device__ __forceinline__ int trace_ray(const DevGeom& G, int a, int c,
 }
 
 // First detector column of the two-column window that holds every ray
-// crossing pixel (x, y) at angle a. A pixel's footprint on the detector is
-// (|sin|+|cos|) <= sqrt(2) wide, so with a 0.25-column margin for the
-// reference's float jitter at most two columns fall in the window. Built and
-// read with the same rounding, so construction and use agree bit for bit.
-__device__ __forceinline__ int window_c0(const DevGeom& G, int a, int x, int y) {
-  const float s = G.sinq[a], c = G.cosq[a];
-  const float px = fadd(fsub((float)x, G.halfg), 0.5f);
-  const float py = fadd(fsub((float)y, G.halfg), 0.5f);
-  const float t = fadd(fmul(-px, s), fmul(py, c));
-  const float hw = fmul(fadd(fabsf(s), fabsf(c)), 0.5f);
-  const float lo = fsub(fsub(fsub(t, hw), 0.25f), G.off);
-  return (int)ceilf(lo);
+// crossing pixel (x, y) at angle a:
+//   c0 = ceil(-sin*x + cos*y + D),
+//   D  = (g/2 - 1/2)(sin - cos) - (|sin| + |cos|)/2 - 1/4 - off,
+// i.e. the detector coordinate of the pixel centre minus half the pixel's
+// footprint (|sin|+|cos| <= sqrt(2) wide) minus a 1/4-column margin for the
+// reference's float jitter, so at most two columns fall in the window.
+// coef = {-sin, cos, D} per angle (host-computed). Construction and use call
+// this same function, so they agree bit for bit.
+__device__ __forceinline__ int window_c0(float4 coef, float xf, float yf) {
+  return (int)ceilf(__fmaf_rn(coef.y, yf, __fmaf_rn(coef.x, xf, coef.z)));
+}
+
+// Backward-matrix position of pixel (x, y): 8x4 pixel tiles, one warp per
+// tile, tiles row-major; entry (angle, tile, lane) is one 32-lane row.
+__device__ __forceinline__ void pixel_tile(int x, int y, int tiles_x, int* tile,
+                                           int* lane) {
+  *tile = (y >> 2) * tiles_x + (x >> 3);
+  *lane = ((y & 3) << 3) | (x & 7);
 }
 
 // ---- segment-length storage -------------------------------------------------
 enum LenKind { LK_F32 = 0, LK_BF16 = 1, LK_F16 = 2, LK_U16 = 3 };
+
+template <int LK>
+__device__ __forceinline__ float decode_len(uint16_t v, float inv_scale) {
+  if constexpr (LK == LK_BF16) return __bfloat162float(__ushort_as_bfloat16(v));
+  else if constexpr (LK == LK_F16) return __half2float(__ushort_as_half(v));
+  else return (float)v * inv_scale;
+}
 
 // 16-bit codes; `kind` is warp-uniform so the switch does not diverge.
 __device__ __forceinline__ float decode16(uint16_t v, int kind, float inv_scale) {
@@ -164,6 +177,12 @@ __device__ __forceinline__ Vec<K> load_vec(const float* p) {
     float2 t = __ldg(reinterpret_cast<const float2*>(p));
     r.v[0] = t.x;
     r.v[1] = t.y;
+  } else if constexpr (K == 8) {
+    // one 256-bit read-only load: a single L1 sector lookup per gather
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3]),
+          "=f"(r.v[4]), "=f"(r.v[5]), "=f"(r.v[6]), "=f"(r.v[7])
+        : "l"(p));
   } else {
 #pragma unroll
     for (int j = 0; j < K; j += 4) {

@@ -22,9 +22,12 @@ struct MatrixDev {
   const int* rstart;      // delta form: [P*C] first pixel of each ray
   const void* rlen;    // length per entry (float or 16-bit code)
   const float* ra2;    // [P*C] sum of squared lengths (SIRT's a2)
-  // backward matrix, (angle, pixel)-major: dlen[(a*g*g + p)*2 + slot] is the
-  // length of ray (a, window_c0(a, p) + slot) through pixel p
+  // backward matrix, angle-major over 8x4 pixel tiles: for pixel (x, y) in
+  // tile t at lane l, dlen[((a*ntiles + t)*32 + l)*2 + slot] is the length of
+  // ray (a, window_c0 + slot) through the pixel
   const void* dlen;
+  const float4* wcoef; // [P] window coefficients {-sin, cos, D, 0}
+  int tiles_x, ntiles;
   const float* W;      // [g*g] total length through each pixel
   int len_kind;        // LenKind
   float scale, inv_scale;
@@ -52,6 +55,25 @@ struct IterArgs {
   PenaltyWeights pw;
 };
 
+// Address of (slot, pixel) in the batched reconstruction layout.
+__device__ __forceinline__ int64_t slot_addr(int slot, int64_t p, int64_t g2,
+                                             int K) {
+  return ((int64_t)(slot / K) * g2 + p) * K + (slot % K);
+}
+
+// APMLR's axial neighbours of slice s: the first slice of the dataset has
+// none above, the last none below (apmlr.cc:937-967).
+__device__ __forceinline__ void apmlr_axial(const IterArgs& A, int s, int* up,
+                                            int* down) {
+  const int beg = A.slice_id, end = A.slice_id + A.S - 1;
+  const int final_index = A.slice_id + A.num_total_slices - 1;
+  const bool top = (beg == 0 && s == 0);
+  const bool bottom =
+      !top && (final_index == end && final_index != 0 && s == A.S - 1);
+  *up = !bottom;
+  *down = !top;
+}
+
 // tg_trace.cu
 void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
                         unsigned* maxlen_bits, cudaStream_t st);
@@ -64,13 +86,15 @@ void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
 void launch_trace_export(const DevGeom& G, const int64_t* offsets, int* idx,
                          float* len, float* len2, cudaStream_t st);
 
-// tg_iter.cu
+// tg_forward.cu
 void launch_forward(const IterArgs& A, const float* recon_batch,
                     const float* sino_batch, float* out, int out_mode,
                     cudaStream_t st);
+// tg_backward.cu
 void launch_backward(const IterArgs& A, int batch, const float* recon_cur,
                      float* recon_next, const float* upd, float* rep_num,
                      int epi, cudaStream_t st);
+// tg_iter.cu
 void launch_fg(const IterArgs& A, const float* recon, const float* W, float* F,
                float* Gv, cudaStream_t st);
 void launch_update(const IterArgs& A, float* recon, const float* W,

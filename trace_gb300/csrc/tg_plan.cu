@@ -24,6 +24,7 @@ struct tg_plan {
   PenaltyWeights pw_base{};
   // device allocations
   float *d_yi = nullptr, *d_sin = nullptr, *d_cos = nullptr;
+  float4* d_wcoef = nullptr;
   int* d_quad = nullptr;
   int64_t *d_roff = nullptr, *d_rcoff = nullptr;
   int *d_rcap = nullptr, *d_rnseg = nullptr, *d_ridx = nullptr, *d_rstart = nullptr;
@@ -363,6 +364,22 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   G.cosq = p->d_cos;
   G.quad = p->d_quad;
 
+  // window coefficients of the backward matrix: c0 = ceil(-s*x + c*y + D)
+  // (tg::window_c0), D from the pixel-centre offset, half the footprint and
+  // a quarter-column margin
+  std::vector<float4> wc(P);
+  const double off = (1.0 - C) / 2.0 + (double)mov;
+  for (int a = 0; a < P; ++a) {
+    const double sd = sn[a], cd = cs[a];
+    const double D = (C / 2.0 - 0.5) * (sd - cd) -
+                     0.5 * (std::fabs(sd) + std::fabs(cd)) - 0.25 - off;
+    wc[a] = make_float4(-sn[a], cs[a], (float)D, 0.f);
+  }
+  if ((rc = dalloc(p, &p->d_wcoef, P))) return bail(rc);
+  cudaMemcpyAsync(p->d_wcoef, wc.data(), P * sizeof(float4),
+                  cudaMemcpyHostToDevice, p->st);
+  const int tiles_x = (C + 7) / 8, tiles_y = (C + 3) / 4;
+
   // pass 1: segment counts, per-group capacity, longest segment
   const int ngroups = P * G.gpa;
   if ((rc = dalloc(p, &p->d_rnseg, (size_t)p->R)) ||
@@ -419,7 +436,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     if ((rc = dalloc(p, &t, (size_t)entries, true))) return bail(rc);
     p->d_rlen = t;
   }
-  const size_t dense_n = (size_t)P * p->g2 * 2;
+  const size_t dense_n = (size_t)P * tiles_x * tiles_y * 32 * 2;
   if (l16) {
     uint16_t* t;
     if ((rc = dalloc(p, &t, dense_n, true))) return bail(rc);
@@ -442,6 +459,9 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   M.rlen = p->d_rlen;
   M.ra2 = p->d_ra2;
   M.dlen = p->d_dlen;
+  M.wcoef = p->d_wcoef;
+  M.tiles_x = tiles_x;
+  M.ntiles = tiles_x * tiles_y;
   M.W = p->d_W;
   M.len_kind = p->len_kind;
   M.scale = maxlen > 0 ? 65535.f / maxlen : 1.f;

@@ -49,9 +49,10 @@ __global__ void __launch_bounds__(kTraceBlock)
   const int c = (grp - a * G.gpa) * 32 + lane;
   if (c >= G.C) return;
   const int g = G.C;
-  const int64_t g2 = (int64_t)g * g;
   const int64_t r = (int64_t)a * G.C + c;
   const int64_t base = M.roff[grp] + lane;
+  const float4 coef = M.wcoef[a];
+  const int64_t abase = (int64_t)a * M.ntiles * 32;
   const int64_t cbase = DELTA ? M.rcoff[grp] + lane : 0;
   float a2 = 0.f;
   int s = 0, pix = 0, piy = 0;
@@ -83,14 +84,16 @@ __global__ void __launch_bounds__(kTraceBlock)
       reinterpret_cast<float*>(rlen)[e] = l;
     a2 = fadd(a2, l2);
     // backward matrix: slot = column offset inside the pixel's window
-    const int slot = c - window_c0(G, a, ix, iy);
+    const int slot = c - window_c0(coef, (float)ix, (float)iy);
     if (slot < 0 || slot > 1) {
       ++bad;
     } else {
       // A present entry never stores +0: a zero length is kept as -0 so the
       // backprojection still visits it (0 * a non-finite factor is NaN in
       // the reference too). The 16-bit fixed-point code has no -0.
-      const int64_t pos = ((int64_t)a * g2 + idx) * 2 + slot;
+      int tile, tl;
+      pixel_tile(ix, iy, M.tiles_x, &tile, &tl);
+      const int64_t pos = (abase + (int64_t)tile * 32 + tl) * 2 + slot;
       if (L16) {
         uint16_t* d = reinterpret_cast<uint16_t*>(dlen);
         const float cur = decode16(d[pos], M.len_kind, M.inv_scale);
@@ -116,12 +119,16 @@ __global__ void __launch_bounds__(kTraceBlock)
 template <bool L16>
 __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W) {
   const int g = G.C;
-  const int64_t g2 = (int64_t)g * g;
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= g2) return;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)M.ntiles * 32) return;
+  const int tile = (int)(t >> 5), lane = (int)(t & 31);
+  const int x = (tile % M.tiles_x) * 8 + (lane & 7);
+  const int y = (tile / M.tiles_x) * 4 + (lane >> 3);
+  if (x >= g || y >= g) return;
+  const int64_t p = (int64_t)y * g + x;
   float sum = 0.f, comp = 0.f;
   for (int a = 0; a < G.P; ++a) {
-    const int64_t pos = ((int64_t)a * g2 + p) * 2;
+    const int64_t pos = ((int64_t)a * M.ntiles * 32 + t) * 2;
     float l0, l1;
     if (L16) {
       const uint32_t w =
@@ -135,14 +142,14 @@ __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W) {
     }
     if (exact) {
       sum = fadd(fadd(sum, l0), l1);
-    } else {
-      float y = l0 - comp, t = sum + y;
-      comp = (t - sum) - y;
-      sum = t;
-      y = l1 - comp;
-      t = sum + y;
-      comp = (t - sum) - y;
-      sum = t;
+    } else {  // compensated (Kahan) sum
+      float yk = l0 - comp, tk = sum + yk;
+      comp = (tk - sum) - yk;
+      sum = tk;
+      yk = l1 - comp;
+      tk = sum + yk;
+      comp = (tk - sum) - yk;
+      sum = tk;
     }
   }
   W[p] = sum;
@@ -197,8 +204,7 @@ void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
 
 void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
                     cudaStream_t st) {
-  const int64_t g2 = (int64_t)G.C * G.C;
-  const int blocks = (int)((g2 + 255) / 256);
+  const int blocks = (int)(((int64_t)M.ntiles * 32 + 255) / 256);
   if (M.len_kind != LK_F32)
     k_weights<true><<<blocks, 256, 0, st>>>(G, M, exact, W);
   else
