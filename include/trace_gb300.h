@@ -185,6 +185,33 @@ int tg_forward_project(tg_plan* plan, int alg, const tg_params* params,
 int tg_trace_rays(tg_plan* plan, int32_t* counts, const int64_t* offsets,
                   int32_t* idx, float* len, float* len2);
 
+/* One slice's reduction (forward projection + backprojection) into caller
+ * buffers, allocating no device memory. No counterpart in the reference: it
+ * exists for callers that must not allocate on the GPU while they run -
+ * hosts that hand the library a fixed memory budget up front and treat any
+ * later allocation as a failure, or latency-sensitive pipelines where a
+ * cudaMalloc/cudaFree (which may synchronize the device) would stall work on
+ * their other streams. The plan itself is created beforehand, as usual.
+ *
+ *   recon: device, C x C floats - the reconstruction the forward projection
+ *          reads (for APMLR's reference behaviour, slice s-1).
+ *   sino:  device, P x C floats - this slice's sinogram rows (|x| applied
+ *          where the driver applies it).
+ *   num:   device, C x C floats - receives replica[2p] for every pixel, the
+ *          values tg_get_replica returns at even positions.
+ * The per-ray factors between the two passes live in one file-scope device
+ * array of 4,194,304 floats (16 MiB, held by every GPU that loads the
+ * library until the process exits); plans with P*C above that return
+ * TG_E_LIMIT. The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress) and caches it, so make that first call before any
+ * stream capture. Every call shares the array: calls whose work overlaps on
+ * the GPU (different streams, or different plans on one device) race on it;
+ * the array needs no clearing, since each call writes every factor it reads.
+ * Work is issued on the plan's stream; the device that was current when the
+ * plan was created must be current. */
+int tg_reduce_slice_noalloc(tg_plan* plan, int alg, const tg_params* params,
+                            const float* recon, const float* sino, float* num);
+
 #ifdef __cplusplus
 }
 #endif

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -817,3 +818,65 @@ int tg_trace_rays(tg_plan* p, int32_t* counts, const int64_t* offsets,
 }
 
 }  // extern "C"
+
+// ---- allocation-free single-slice reduce ------------------------------------
+// For callers that may not allocate device memory while they run (see the
+// declaration in trace_gb300.h): the per-ray factors the forward pass hands
+// to the backprojection go to this fixed array instead of the plan's buffer.
+namespace {
+
+constexpr int64_t kNoAllocMaxRays = int64_t(1) << 22;  // 4,194,304 floats
+static __device__ __align__(256) float g_noalloc_factors[kNoAllocMaxRays];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+float* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of the array on the current device, looked up once per
+// device. In host code the array's name is only a host-side stand-in.
+int noalloc_factors(tg_plan* p, float** out) {
+  int dev = -1;
+  TG_CUDA(p, cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return fail(p, TG_E_LIMIT, "device ordinal outside 0..63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* addr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_factors);
+    if (e != cudaSuccess || !addr)
+      return fail(p, TG_E_CUDA,
+                  std::string("cudaGetSymbolAddress of the factor array: ") +
+                      cudaGetErrorString(e));
+    g_noalloc_addr[dev] = static_cast<float*>(addr);
+  }
+  *out = g_noalloc_addr[dev];
+  return TG_OK;
+}
+
+}  // namespace
+
+extern "C" int tg_reduce_slice_noalloc(tg_plan* p, int alg,
+                                       const tg_params* prm, const float* recon,
+                                       const float* sino, float* num) {
+  if (!p) return TG_E_ARG;
+  if (!recon || !sino || !num) return fail(p, TG_E_ARG, "null device buffer");
+  if (!valid_alg(alg)) return fail(p, TG_E_ARG, "unknown algorithm");
+  if (p->R > kNoAllocMaxRays)
+    return fail(p, TG_E_LIMIT,
+                "P*C = " + std::to_string(p->R) +
+                    " rays exceeds the 4,194,304-ray factor array of "
+                    "tg_reduce_slice_noalloc");
+  float* factors = nullptr;
+  TG_TRY(noalloc_factors(p, &factors));
+  IterArgs A = make_args(p, alg, prm);
+  A.K = 1;  // one slice: plain [C*C] / [P*C] layouts
+  A.S = 1;
+  A.vshift = 0;
+  A.fshift = 0;
+  A.nslots = 1;
+  launch_forward(A, recon, sino, factors, alg == TG_SIRT ? FWD_SIRT : FWD_RATIO,
+                 p->st);
+  launch_backward(A, 0, recon, nullptr, factors, num, EPI_REPLICA, p->st);
+  TG_CUDA(p, cudaGetLastError());
+  return TG_OK;
+}
