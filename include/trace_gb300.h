@@ -74,7 +74,10 @@ enum tg_len_storage {
 enum tg_mode {
   TG_MODE_EXACT = 0, /* reference operation order, IEEE-rounded mul/add/div:
                         forward ray sums are bit-identical to the reference */
-  TG_MODE_FAST = 1   /* fused multiply-add and compensated (Kahan) sums */
+  TG_MODE_FAST = 1,  /* fused multiply-add accumulation */
+  TG_MODE_FP64 = 2   /* reconstruction, factors, sums and updates in double
+                        (f32 lengths, one slice per pass, tg_iterate only):
+                        the FP64 run errors are measured against */
 };
 
 typedef struct {

@@ -84,3 +84,14 @@ def test_plan_creation_fails_loudly_without_gpu(lib):
     with pytest.raises(tg.TraceError) as e:
         tg.Plan(8, 1, 16, np.zeros(8, np.float32))
     assert "CUDA" in str(e.value) or "E_CUDA" in str(e.value)
+
+
+def test_driver_builds_and_rejects_bad_usage(lib):
+    import subprocess
+    drv = tgb.build_driver()
+    r = subprocess.run([drv], capture_output=True, text=True)
+    assert r.returncode == 1 and "need" in r.stderr
+    r = subprocess.run([drv, "-r", "sirt", "-f", "/nonexistent", "-t", "/nonexistent",
+                        "-o", "/tmp/x", "-P", "4", "-S", "1", "-C", "8"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "cannot open" in r.stderr

@@ -23,7 +23,7 @@ from .build import LIB as LIB_PATH
 
 ALGS = {"sirt": 0, "mlem": 1, "pml": 2, "apmlr": 3}
 LEN_STORAGE = {"f32": 0, "bf16": 1, "f16": 2, "u16": 3}
-MODES = {"exact": 0, "fast": 1}
+MODES = {"exact": 0, "fast": 1, "fp64": 2}
 STATUS = {0: "OK", 1: "E_ARG", 2: "E_CUDA", 3: "E_NOMEM", 4: "E_STATE",
           5: "E_GEOMETRY", 6: "E_LIMIT"}
 

@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libtrace_gb300.so")
-SOURCES = ["tg_trace.cu", "tg_forward.cu", "tg_backward.cu", "tg_iter.cu", "tg_plan.cu"]
+SOURCES = ["tg_trace.cu", "tg_forward.cu", "tg_backward.cu", "tg_iter.cu", "tg_fp64.cu", "tg_plan.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -42,6 +42,25 @@ def _compile(src: str, extra=()) -> str:
     return obj
 
 
+DRIVER = os.path.join(OUT, "trace_recon")
+
+
+def build_driver() -> str:
+    """The C++ reconstruction driver over the drop-in classes."""
+    src = os.path.join(HERE, "host", "trace_recon.cc")
+    hdr = os.path.join(HERE, "host", "trace_gb300.hpp")
+    if (os.path.exists(DRIVER) and os.path.getmtime(DRIVER) > max(
+            os.path.getmtime(src), os.path.getmtime(hdr), os.path.getmtime(LIB))):
+        return DRIVER
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", src, "-o", DRIVER, f"-L{OUT}",
+           "-ltrace_gb300", f"-Wl,-rpath,{OUT}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    return DRIVER
+
+
 def build(verbose: bool = False, extra=()) -> str:
     os.makedirs(OUT, exist_ok=True)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
@@ -49,6 +68,7 @@ def build(verbose: bool = False, extra=()) -> str:
     if os.path.exists(LIB) and not extra:
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) < t for d in deps):
+            build_driver()
             return LIB
     with cf.ThreadPoolExecutor(len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
@@ -58,6 +78,7 @@ def build(verbose: bool = False, extra=()) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver()
     if verbose:
         print("built", LIB)
     return LIB

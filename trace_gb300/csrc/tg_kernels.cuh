@@ -79,7 +79,7 @@ void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
                         unsigned* maxlen_bits, cudaStream_t st);
 void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
                        uint32_t* rcode, int* rstart, void* rlen, float* ra2,
-                       void* dlen, unsigned long long* overflow,
+                       double* ra2d, void* dlen, unsigned long long* overflow,
                        cudaStream_t st);
 void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
                     cudaStream_t st);
@@ -94,6 +94,18 @@ void launch_forward(const IterArgs& A, const float* recon_batch,
 void launch_backward(const IterArgs& A, int batch, const float* recon_cur,
                      float* recon_next, const float* upd, float* rep_num,
                      int epi, cudaStream_t st);
+// tg_fp64.cu
+void launch_forward64(const IterArgs& A, const double* ra2d, const double* recon,
+                      const float* sino, double* out, int out_mode,
+                      cudaStream_t st);
+void launch_backward64(const IterArgs& A, int s, const double* cur,
+                       double* next, const double* upd, const double* W,
+                       cudaStream_t st);
+void launch_weights64(const DevGeom& G, const MatrixDev& M, double* W,
+                      cudaStream_t st);
+void launch_convert(const float* in, double* out, int64_t n, cudaStream_t st);
+void launch_narrow(const double* in, float* out, int64_t n, cudaStream_t st);
+void launch_fill64(double* p, int64_t n, double v, cudaStream_t st);
 // tg_iter.cu
 void launch_fg(const IterArgs& A, const float* recon, const float* W, float* F,
                float* Gv, cudaStream_t st);

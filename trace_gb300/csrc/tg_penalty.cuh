@@ -67,50 +67,71 @@ __device__ __forceinline__ int nbr_class(int x, int y, int g, int* region) {
   return 0;
 }
 
+// Rounded arithmetic for the penalty in the reconstruction's type: float
+// keeps the reference's individually rounded single operations, double is
+// the FP64 mode.
+template <class T> struct Ar;
+template <> struct Ar<float> {
+  static __device__ __forceinline__ float mul(float a, float b) { return fmul(a, b); }
+  static __device__ __forceinline__ float add(float a, float b) { return fadd(a, b); }
+  static __device__ __forceinline__ float sub(float a, float b) { return fsub(a, b); }
+  static __device__ __forceinline__ float div(float a, float b) { return fdiv(a, b); }
+  static __device__ __forceinline__ float sqrt(float a) { return fsqrt(a); }
+  static __device__ __forceinline__ float abs(float a) { return fabsf(a); }
+};
+template <> struct Ar<double> {
+  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+  static __device__ __forceinline__ double sqrt(double a) { return __dsqrt_rn(a); }
+  static __device__ __forceinline__ double abs(double a) { return ::fabs(a); }
+};
+
 // F and G (before G += sum of lengths) of one pixel.
 //   rec(dx, dy, dz): the iteration's input reconstruction at the neighbour
 //   offset (dz = axial slice offset, APMLR only).
 //   up / down: APMLR axial neighbours at +1 / -1 slice present.
-template <class Rec>
+template <class T, class Rec>
 __device__ __forceinline__ void penalty_fg(bool apmlr, const PenaltyWeights& W,
                                            int x, int y, int g, int up,
-                                           int down, Rec&& rec, float& F,
-                                           float& G) {
+                                           int down, Rec&& rec, T& F, T& G) {
+  using A = Ar<T>;
   int region;
   const int cls = nbr_class(x, y, g, &region);
-  const float r0 = rec(0, 0, 0);
-  float f = 0.f, gg = 0.f;
+  const T r0 = rec(0, 0, 0);
+  T f = 0, gg = 0;
   const int n = c_nbr.n[cls];
   if (!apmlr) {
-    const float twob = fmul(2.f, W.beta);
+    const T twob = A::mul(T(2), T(W.beta));
     for (int q = 0; q < n; ++q) {
-      const float w = W.pml[region][c_nbr.kind[cls][q]];
-      const float rq = rec(c_nbr.dx[cls][q], c_nbr.dy[cls][q], 0);
-      const float tw = fmul(twob, w);
-      f = fadd(f, tw);
-      gg = fsub(gg, fmul(tw, fadd(r0, rq)));
+      const T w = W.pml[region][c_nbr.kind[cls][q]];
+      const T rq = rec(c_nbr.dx[cls][q], c_nbr.dy[cls][q], 0);
+      const T tw = A::mul(twob, w);
+      f = A::add(f, tw);
+      gg = A::sub(gg, A::mul(tw, A::add(r0, rq)));
     }
   } else {
     const int nax = up + down;
     const float* w = W.apmlr[region][nax == 2 ? 0 : 1];
-    const float twob = fmul(2.f, W.beta), twob1 = fmul(2.f, W.beta1);
+    const T twob = A::mul(T(2), T(W.beta)), twob1 = A::mul(T(2), T(W.beta1));
     for (int q = 0; q < n; ++q) {
-      const float wq = w[c_nbr.kind[cls][q]];
-      const float rq = rec(c_nbr.dx[cls][q], c_nbr.dy[cls][q], 0);
-      const float mg = fadd(r0, rq), rg = fsub(r0, rq);
-      const float gam = fdiv(1.f, fadd(1.f, fabsf(fdiv(rg, W.delta))));
-      const float t = fmul(fmul(twob, wq), gam);
-      f = fadd(f, t);
-      gg = fsub(gg, fmul(t, mg));
+      const T wq = w[c_nbr.kind[cls][q]];
+      const T rq = rec(c_nbr.dx[cls][q], c_nbr.dy[cls][q], 0);
+      const T mg = A::add(r0, rq), rg = A::sub(r0, rq);
+      const T gam = A::div(T(1), A::add(T(1), A::abs(A::div(rg, T(W.delta)))));
+      const T t = A::mul(A::mul(twob, wq), gam);
+      f = A::add(f, t);
+      gg = A::sub(gg, A::mul(t, mg));
     }
     for (int q = 0; q < 2; ++q) {
       if (q == 0 ? !up : !down) continue;
-      const float rq = rec(0, 0, q == 0 ? 1 : -1);
-      const float mg = fadd(r0, rq), rg = fsub(r0, rq);
-      const float gam = fdiv(1.f, fadd(1.f, fabsf(fdiv(rg, W.delta1))));
-      const float t = fmul(fmul(twob1, w[2]), gam);
-      f = fadd(f, t);
-      gg = fsub(gg, fmul(t, mg));
+      const T rq = rec(0, 0, q == 0 ? 1 : -1);
+      const T mg = A::add(r0, rq), rg = A::sub(r0, rq);
+      const T gam = A::div(T(1), A::add(T(1), A::abs(A::div(rg, T(W.delta1)))));
+      const T t = A::mul(A::mul(twob1, T(w[2])), gam);
+      f = A::add(f, t);
+      gg = A::sub(gg, A::mul(t, mg));
     }
   }
   F = f;
@@ -118,9 +139,11 @@ __device__ __forceinline__ void penalty_fg(bool apmlr, const PenaltyWeights& W,
 }
 
 // Closed-form root of UpdateRecon (pml.cc:18-20, apmlr.cc:20-22).
-__device__ __forceinline__ float penalised_root(float F, float G, float num) {
-  const float disc = fsub(fmul(G, G), fmul(fmul(8.f, num), F));
-  return fdiv(fadd(-G, fsqrt(disc)), fmul(4.f, F));
+template <class T>
+__device__ __forceinline__ T penalised_root(T F, T G, T num) {
+  using A = Ar<T>;
+  const T disc = A::sub(A::mul(G, G), A::mul(A::mul(T(8), num), F));
+  return A::div(A::add(-G, A::sqrt(disc)), A::mul(T(4), F));
 }
 
 }  // namespace tg

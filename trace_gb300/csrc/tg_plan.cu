@@ -34,6 +34,9 @@ struct tg_plan {
   float* d_ra2 = nullptr;
   void* d_dlen = nullptr;
   float* d_W = nullptr;
+  // FP64 mode: double state, factors, total lengths and SIRT's a2
+  bool fp64 = false;
+  double *d_ra2d = nullptr, *d_W64 = nullptr;
   unsigned* d_maxlen = nullptr;
   unsigned long long* d_overflow = nullptr;
   float* d_sino = nullptr;
@@ -211,13 +214,14 @@ int establish_layout(tg_plan* p, int alg) {
   const int nslots = (need + p->K - 1) / p->K * p->K;
   if (p->layout_alg < 0 || p->nslots != nslots || p->halo != halo ||
       p->vshift != vshift) {
-    const size_t old_n = (size_t)p->nslots * p->g2;
+    const size_t esz = p->fp64 ? 2 : 1;  // floats per element
+    const size_t old_n = (size_t)p->nslots * p->g2 * esz;
     for (int b = 0; b < 2; ++b) {
       dfree(p, p->d_recon[b], old_n * sizeof(float));
       p->d_recon[b] = nullptr;
     }
     for (int b = 0; b < 2; ++b)
-      TG_TRY(dalloc(p, &p->d_recon[b], (size_t)nslots * p->g2));
+      TG_TRY(dalloc(p, &p->d_recon[b], (size_t)nslots * p->g2 * esz));
   }
   p->halo = halo;
   p->vshift = vshift;
@@ -262,8 +266,18 @@ float* batch_ptr(tg_plan* p, float* base, int batch_slot) {
 
 int ensure_upd(tg_plan* p) {
   if (p->d_upd) return TG_OK;
-  return dalloc(p, &p->d_upd, (size_t)p->R * p->K);
+  return dalloc(p, &p->d_upd, (size_t)p->R * p->K * (p->fp64 ? 2 : 1));
 }
+
+int fp32_only(tg_plan* p) {
+  if (p->fp64)
+    return fail(p, TG_E_STATE,
+                "FP64 plans support tg_iterate and reconstruction upload/"
+                "download only");
+  return TG_OK;
+}
+
+double* as_f64(float* p) { return reinterpret_cast<double*>(p); }
 
 }  // namespace
 
@@ -295,8 +309,12 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     return fail(nullptr, TG_E_ARG, "slices_per_pass must be 1, 2, 4 or 8");
   if (d.len_storage < TG_LEN_F32 || d.len_storage > TG_LEN_U16)
     return fail(nullptr, TG_E_ARG, "unknown len_storage");
-  if (d.mode != TG_MODE_EXACT && d.mode != TG_MODE_FAST)
+  if (d.mode != TG_MODE_EXACT && d.mode != TG_MODE_FAST && d.mode != TG_MODE_FP64)
     return fail(nullptr, TG_E_ARG, "unknown mode");
+  if (d.mode == TG_MODE_FP64 &&
+      (d.len_storage != TG_LEN_F32 || d.slices_per_pass != 1 || d.delta_index))
+    return fail(nullptr, TG_E_ARG,
+                "FP64 mode needs f32 lengths, explicit indices and one slice per pass");
   if ((sin_tab == nullptr) != (cos_tab == nullptr))
     return fail(nullptr, TG_E_ARG, "give both sin_tab and cos_tab or neither");
 
@@ -312,6 +330,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   p->R = (int64_t)p->P * p->C;
   p->len_kind = d.len_storage;
   p->nb = (p->S + p->K - 1) / p->K;
+  p->fp64 = d.mode == TG_MODE_FP64;
 
   auto bail = [&](int rc) {
     g_create_error = p->err;
@@ -448,6 +467,9 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     p->d_dlen = t;
   }
   if ((rc = dalloc(p, &p->d_W, (size_t)p->g2))) return bail(rc);
+  if (p->fp64 && ((rc = dalloc(p, &p->d_ra2d, (size_t)p->R)) ||
+                  (rc = dalloc(p, &p->d_W64, (size_t)p->g2))))
+    return bail(rc);
 
   MatrixDev& M = p->M;
   M.roff = p->d_roff;
@@ -470,8 +492,9 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
 
   // pass 2: fill both matrices; pass 3: total length per pixel
   launch_trace_fill(G, M, p->d_ridx, p->d_rcode, p->d_rstart, p->d_rlen,
-                    p->d_ra2, p->d_dlen, p->d_overflow, p->st);
+                    p->d_ra2, p->d_ra2d, p->d_dlen, p->d_overflow, p->st);
   launch_weights(G, M, d.mode == TG_MODE_EXACT, p->d_W, p->st);
+  if (p->fp64) launch_weights64(G, M, p->d_W64, p->st);
   unsigned long long overflow = 0;
   cudaMemcpyAsync(&overflow, p->d_overflow, 8, cudaMemcpyDeviceToHost, p->st);
   cudaEventRecord(e1, p->st);
@@ -604,8 +627,12 @@ int tg_reset_recon(tg_plan* p, int alg) {
   if (!p) return TG_E_ARG;
   TG_TRY(establish_layout(p, alg));
   const float init = alg == TG_SIRT ? 0.f : 1.f;
-  for (int b = 0; b < 2; ++b)
-    launch_fill(p->d_recon[b], (size_t)p->nslots * p->g2, init, p->st);
+  for (int b = 0; b < 2; ++b) {
+    if (p->fp64)
+      launch_fill64(as_f64(p->d_recon[b]), (int64_t)p->nslots * p->g2, init, p->st);
+    else
+      launch_fill(p->d_recon[b], (size_t)p->nslots * p->g2, init, p->st);
+  }
   TG_CUDA(p, cudaGetLastError());
   return TG_OK;
 }
@@ -622,9 +649,14 @@ int tg_set_recon(tg_plan* p, int alg, const float* recon, int on_device) {
                                cudaMemcpyHostToDevice, p->st));
     src = p->d_stage;
   }
-  for (int b = 0; b < 2; ++b)
-    launch_recon_pack(src, p->d_recon[b], nuser, (int)p->g2, p->K,
-                      p->vshift - p->halo, p->nslots, p->st);
+  for (int b = 0; b < 2; ++b) {
+    if (p->fp64)
+      launch_convert(src, as_f64(p->d_recon[b]) + (int64_t)(p->vshift - p->halo) * p->g2,
+                     (int64_t)n, p->st);
+    else
+      launch_recon_pack(src, p->d_recon[b], nuser, (int)p->g2, p->K,
+                        p->vshift - p->halo, p->nslots, p->st);
+  }
   TG_CUDA(p, cudaGetLastError());
   return TG_OK;
 }
@@ -639,8 +671,12 @@ int tg_get_recon(tg_plan* p, int alg, float* recon, int on_device) {
     TG_TRY(stage(p, n));
     dst = p->d_stage;
   }
-  launch_recon_unpack(p->d_recon[p->cur], dst, nuser, (int)p->g2, p->K,
-                      p->vshift - p->halo, p->st);
+  if (p->fp64)
+    launch_narrow(as_f64(p->d_recon[p->cur]) + (int64_t)(p->vshift - p->halo) * p->g2,
+                  dst, (int64_t)n, p->st);
+  else
+    launch_recon_unpack(p->d_recon[p->cur], dst, nuser, (int)p->g2, p->K,
+                        p->vshift - p->halo, p->st);
   TG_CUDA(p, cudaGetLastError());
   if (!on_device) {
     TG_CUDA(p, cudaMemcpyAsync(recon, p->d_stage, n * sizeof(float),
@@ -667,6 +703,25 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
   TG_TRY(ensure_upd(p));
   const IterArgs A = make_args(p, alg, prm);
   const int mode = alg == TG_SIRT ? FWD_SIRT : FWD_RATIO;
+  if (p->fp64) {
+    for (int it = 0; it < n_iter; ++it) {
+      const double* cur = as_f64(p->d_recon[p->cur]);
+      double* next = as_f64(p->d_recon[p->cur ^ 1]);
+      double* upd = as_f64(p->d_upd);
+      for (int s = 0; s < p->S; ++s) {
+        {
+          Timed t(p, 0);
+          launch_forward64(A, p->d_ra2d, cur + (int64_t)(s + p->fshift) * p->g2,
+                           p->d_sino + (int64_t)s * p->R, upd, mode, p->st);
+        }
+        Timed t(p, 1);
+        launch_backward64(A, s, cur, next, upd, p->d_W64, p->st);
+      }
+      p->cur ^= 1;
+    }
+    TG_CUDA(p, cudaGetLastError());
+    return TG_OK;
+  }
   for (int it = 0; it < n_iter; ++it) {
     for (int b = 0; b < p->nb; ++b) {
       run_forward(p, A, b, mode, p->d_upd);
@@ -682,6 +737,7 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
 
 int tg_reduce(tg_plan* p, int alg, const tg_params* prm) {
   if (!p) return TG_E_ARG;
+  TG_TRY(fp32_only(p));
   TG_TRY(check_layout(p, alg));
   if (!p->have_sino) return fail(p, TG_E_STATE, "no sinogram uploaded");
   TG_TRY(ensure_upd(p));
@@ -727,6 +783,7 @@ int tg_reset_replica(tg_plan* p) {
 
 int tg_calculate_fg(tg_plan* p, int alg, const tg_params* prm) {
   if (!p) return TG_E_ARG;
+  TG_TRY(fp32_only(p));
   TG_TRY(check_layout(p, alg));
   if (alg < TG_PML) return fail(p, TG_E_ARG, "CalculateFG exists for PML and APMLR only");
   if (!prm) return fail(p, TG_E_ARG, "null params");
@@ -754,6 +811,7 @@ int tg_get_fg(tg_plan* p, float* F, float* G, int on_device) {
 
 int tg_update_recon(tg_plan* p, int alg, const tg_params* prm) {
   if (!p) return TG_E_ARG;
+  TG_TRY(fp32_only(p));
   TG_TRY(check_layout(p, alg));
   if (!p->d_rep) return fail(p, TG_E_STATE, "no replica: call tg_reduce first");
   if (alg >= TG_PML && !p->d_F)
@@ -773,6 +831,7 @@ int tg_update_recon(tg_plan* p, int alg, const tg_params* prm) {
 int tg_forward_project(tg_plan* p, int alg, const tg_params* prm, float* sim,
                        int on_device) {
   if (!p || !sim) return p ? fail(p, TG_E_ARG, "null output") : TG_E_ARG;
+  TG_TRY(fp32_only(p));
   TG_TRY(check_layout(p, alg));
   const size_t packed = (size_t)p->nb * p->R * p->K;
   const size_t n = (size_t)p->P * p->S * p->C;
@@ -861,6 +920,7 @@ extern "C" int tg_reduce_slice_noalloc(tg_plan* p, int alg,
   if (!p) return TG_E_ARG;
   if (!recon || !sino || !num) return fail(p, TG_E_ARG, "null device buffer");
   if (!valid_alg(alg)) return fail(p, TG_E_ARG, "unknown algorithm");
+  TG_TRY(fp32_only(p));
   if (p->R > kNoAllocMaxRays)
     return fail(p, TG_E_LIMIT,
                 "P*C = " + std::to_string(p->R) +

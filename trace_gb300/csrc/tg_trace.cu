@@ -41,7 +41,7 @@ template <bool L16, bool DELTA>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_fill(DevGeom G, MatrixDev M, int ngroups, int* ridx,
                  uint32_t* rcode, int* rstart, void* rlen, float* ra2,
-                 void* dlen, unsigned long long* overflow) {
+                 double* ra2d, void* dlen, unsigned long long* overflow) {
   const int grp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (grp >= ngroups) return;
@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(kTraceBlock)
   const int64_t abase = (int64_t)a * M.ntiles * 32;
   const int64_t cbase = DELTA ? M.rcoff[grp] + lane : 0;
   float a2 = 0.f;
+  double a2d = 0.0;
   int s = 0, pix = 0, piy = 0;
   uint32_t word = 0;
   unsigned long long bad = 0;
@@ -83,6 +84,7 @@ __global__ void __launch_bounds__(kTraceBlock)
     else
       reinterpret_cast<float*>(rlen)[e] = l;
     a2 = fadd(a2, l2);
+    a2d = __dadd_rn(a2d, (double)l2);
     // backward matrix: slot = column offset inside the pixel's window
     const int slot = c - window_c0(coef, (float)ix, (float)iy);
     if (slot < 0 || slot > 1) {
@@ -111,6 +113,7 @@ __global__ void __launch_bounds__(kTraceBlock)
   if (DELTA && (s & 7) != 0 && s > 0)
     rcode[cbase + (int64_t)(s >> 3) * 32] = word;
   ra2[r] = a2;
+  if (ra2d) ra2d[r] = a2d;
   if (bad) atomicAdd(overflow, bad);
 }
 
@@ -182,7 +185,7 @@ void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
 
 void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
                        uint32_t* rcode, int* rstart, void* rlen, float* ra2,
-                       void* dlen, unsigned long long* overflow,
+                       double* ra2d, void* dlen, unsigned long long* overflow,
                        cudaStream_t st) {
   const int ngroups = G.P * G.gpa;
   const int blocks = (ngroups * 32 + kTraceBlock - 1) / kTraceBlock;
@@ -190,16 +193,16 @@ void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
   const bool delta = rcode != nullptr;
   if (l16 && delta)
     k_trace_fill<true, true><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, dlen, overflow);
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow);
   else if (l16)
     k_trace_fill<true, false><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, dlen, overflow);
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow);
   else if (delta)
     k_trace_fill<false, true><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, dlen, overflow);
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow);
   else
     k_trace_fill<false, false><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, dlen, overflow);
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow);
 }
 
 void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
