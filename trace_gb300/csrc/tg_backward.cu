@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(kBlock, 6)
                  },
                  F, Gv);
       Gv = fadd(Gv, Wp);
-      nv = penalised_root(F, Gv, num);
+      nv = EXACT ? penalised_root(F, Gv, num) : penalised_root_stable(F, Gv, num);
     }
     next[at] = nv;
   }

@@ -51,7 +51,8 @@ __global__ void k_update(IterArgs A, float* __restrict__ recon,
   else if (A.alg == 1)
     recon[at] = fmul(recon[at], fdiv(num, W[p]));
   else
-    recon[at] = penalised_root(F[i], Gv[i], num);
+    recon[at] = A.exact ? penalised_root(F[i], Gv[i], num)
+                        : penalised_root_stable(F[i], Gv[i], num);
 }
 
 // ---- layouts -----------------------------------------------------------------
