@@ -252,11 +252,14 @@ def time_iterations(plan, alg, prm, n, stream_ptr, torch):
     return ev0.elapsed_time(ev1)
 
 
-def kernel_bytes(info, W, K, S_batch_slices, pen=True):
+def kernel_bytes(info, W, K, tiles, pen=True):
     """Algorithmic bytes per launch of the forward and backward kernels."""
     C, P = W["C"], W["P"]
     R, g2 = P * C, C * C
-    fwd = info["forward_bytes"] + 4 * R * K * 2 + 4 * g2 * K
+    if tiles:  # tile stream + one read of the batch + the ray sums written
+        fwd = info["tile_bytes"] + 4 * g2 * K + 4 * R * K
+    else:      # matrix + sinogram in, factors out, batch read once
+        fwd = info["forward_bytes"] + 4 * R * K * 2 + 4 * g2 * K
     back = (info["backward_bytes"] + 4 * R * K + 4 * g2 * K * 2 + 4 * g2
             + (4 * g2 * K if pen else 0))
     return fwd, back
@@ -287,7 +290,7 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     # ---- mixed-precision batched path (the measured value)
     t0 = time.time()
     plan = tg.Plan(P, S, C, theta, len_storage=args.len_storage, slices_per_pass=K,
-                   mode="fast", delta_index=True)
+                   mode="fast", delta_index=True, forward_tiles=args.tiles)
     plan.set_stream(stream)
     info = plan.info()
     sino = make_data(W, dev, plan)
@@ -309,13 +312,14 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     slice_iters = S * args.steps * ws
     value = slice_iters / (ms_max / 1000.0)
     nb = info["batches"]
-    launches = args.steps * nb * 2
+    launches = args.steps * nb * (3 if args.tiles else 2)
 
-    fwd_b, back_b = kernel_bytes(info, W, K, S)
+    fwd_b, back_b = kernel_bytes(info, W, K, args.tiles)
     fwd_avg = tim["forward_ms"] / max(tim["forward_launches"], 1)
     back_avg = tim["backward_ms"] / max(tim["backward_launches"], 1)
     dom = "backward" if tim["backward_ms"] >= tim["forward_ms"] else "forward"
-    kname = {"forward": "k_forward", "backward": "k_backward"}[dom]
+    kname = {"forward": "k_forward_tiled" if args.tiles else "k_forward",
+             "backward": "k_backward"}[dom]
     dom_bytes, dom_ms = (back_b, back_avg) if dom == "backward" else (fwd_b, fwd_avg)
     achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
     traffic = ncu_traffic().get(f"{kname}:{args.workload}:{args.len_storage}:K{K}")
@@ -327,8 +331,10 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
         "share": (tim["backward_ms"] if dom == "backward" else tim["forward_ms"]) /
                  max(tim["forward_ms"] + tim["backward_ms"], 1e-9),
         "kernels": {
-            "k_forward": {"avg_ms": fwd_avg, "bytes": fwd_b,
-                          "gbs": fwd_b / (fwd_avg / 1e3) / 1e9 if fwd_avg else None},
+            ("k_forward_tiled" if args.tiles else "k_forward"): {
+                "avg_ms": fwd_avg, "bytes": fwd_b,
+                "gbs": fwd_b / (fwd_avg / 1e3) / 1e9 if fwd_avg else None},
+            "k_fwd_finish": {"avg_ms": tim["other_ms"] / max(tim["other_launches"], 1)},
             "k_backward": {"avg_ms": back_avg, "bytes": back_b,
                            "gbs": back_b / (back_avg / 1e3) / 1e9 if back_avg else None},
         },
@@ -372,6 +378,8 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
                 "projected by the plan's projector",
         "config": {"workload": W["name"], "slices_per_pass": K,
                    "len_storage": args.len_storage, "index": "4-bit delta",
+                   "forward": "tile-staged (64x64 shared-memory tiles)" if args.tiles
+                              else "ray-ordered",
                    "step": f"one PML iteration over all {S} slices",
                    "l2": "inputs larger than L2 (system matrix "
                          f"{(info['forward_bytes'] + info['backward_bytes']) / 1e9:.1f} GB "
@@ -397,7 +405,8 @@ def fp64_check(args, W, theta, sino, prm, tg, torch, dev):
     sub = sino[:, :n, :].contiguous()
     configs = {
         "fp64": dict(len_storage="f32", mode="fp64"),
-        "mixed": dict(len_storage=args.len_storage, mode="fast", delta_index=True),
+        "mixed": dict(len_storage=args.len_storage, mode="fast", delta_index=True,
+                      forward_tiles=args.tiles),
         "plain_fp32": dict(len_storage="f32", mode="exact"),
     }
     runs = {}
@@ -455,7 +464,7 @@ def end_to_end(args, W, theta, sino, prm, tg, torch, stream):
         t = time.perf_counter()
         p = tg.Plan(W["P"], W["S"], W["C"], theta, len_storage=args.len_storage,
                     slices_per_pass=args.slices_per_pass, mode="fast",
-                    delta_index=True)
+                    delta_index=True, forward_tiles=args.tiles)
         p.set_stream(stream)
         p.set_sinogram(host, apply_abs=True)
         p.reset_recon("pml")
@@ -483,6 +492,8 @@ def main():
     ap.add_argument("--workload", default="pml2048", choices=sorted(WORKLOADS))
     ap.add_argument("--len-storage", default="u16", choices=["u16", "f16", "bf16", "f32"])
     ap.add_argument("--slices-per-pass", type=int, default=8)
+    ap.add_argument("--no-tiles", dest="tiles", action="store_false",
+                    help="ray-ordered forward projection instead of the tile-staged one")
     ap.add_argument("--no-plain", dest="plain", action="store_false")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")

@@ -94,6 +94,10 @@ typedef struct {
   int apmlr_fixed_offset; /* APMLR only. 0 = reference behaviour: the forward
                              projection of slice s reads reconstruction slice
                              s-1 (apmlr.cc:1083-1084); 1 = reads slice s */
+  int forward_tiles;      /* fast mode only: tg_iterate runs the forward
+                             projection through 64x64 reconstruction tiles
+                             staged in shared memory (an extra tile-ordered
+                             copy of the forward matrix is built) */
 } tg_plan_desc;
 
 typedef struct {
@@ -112,6 +116,8 @@ typedef struct {
   float max_segment_length;
   double setup_ms;            /* time spent tracing and building matrices */
   int batches;                /* ceil(stored slices / slices_per_pass) */
+  int64_t tile_bytes;         /* bytes of the tile-ordered forward matrix */
+  int64_t tile_runs;          /* runs (ray pieces inside one tile) */
 } tg_plan_info;
 
 typedef struct {

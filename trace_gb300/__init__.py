@@ -50,7 +50,7 @@ class PlanDesc(C.Structure):
                 ("slice_id", C.c_int), ("num_total_slices", C.c_int),
                 ("len_storage", C.c_int), ("slices_per_pass", C.c_int),
                 ("mode", C.c_int), ("delta_index", C.c_int),
-                ("apmlr_fixed_offset", C.c_int)]
+                ("apmlr_fixed_offset", C.c_int), ("forward_tiles", C.c_int)]
 
 
 class Params(C.Structure):
@@ -62,7 +62,8 @@ class PlanInfo(C.Structure):
     _fields_ = [("num_segments", C.c_int64), ("forward_bytes", C.c_int64),
                 ("backward_bytes", C.c_int64), ("device_bytes", C.c_int64),
                 ("max_segment_length", C.c_float), ("setup_ms", C.c_double),
-                ("batches", C.c_int)]
+                ("batches", C.c_int), ("tile_bytes", C.c_int64),
+                ("tile_runs", C.c_int64)]
 
 
 class Timing(C.Structure):
@@ -122,7 +123,8 @@ class Plan:
     def __init__(self, num_projs, num_slices, num_cols, theta, *, center=0.0,
                  len_storage="f32", slices_per_pass=1, mode="exact",
                  delta_index=False, apmlr_fixed_offset=False, slice_id=0,
-                 num_total_slices=None, sin_tab=None, cos_tab=None):
+                 num_total_slices=None, sin_tab=None, cos_tab=None,
+                 forward_tiles=False):
         self._lib = load_library()
         self.P, self.S, self.C = int(num_projs), int(num_slices), int(num_cols)
         d = PlanDesc(self.P, self.S, self.C, float(center), int(slice_id),
@@ -130,7 +132,8 @@ class Plan:
                      LEN_STORAGE[len_storage] if isinstance(len_storage, str) else int(len_storage),
                      int(slices_per_pass),
                      MODES[mode] if isinstance(mode, str) else int(mode),
-                     int(bool(delta_index)), int(bool(apmlr_fixed_offset)))
+                     int(bool(delta_index)), int(bool(apmlr_fixed_offset)),
+                     int(bool(forward_tiles)))
         theta = np.ascontiguousarray(theta, np.float32)
         if theta.size != self.P:
             raise ValueError("theta must have num_projs entries")

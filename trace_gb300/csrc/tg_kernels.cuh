@@ -33,6 +33,22 @@ struct MatrixDev {
   float scale, inv_scale;
 };
 
+// Tile-staged forward matrix (tg_tiles.cu): per 64x64 tile, groups of 32
+// runs (consecutive segments of one ray inside the tile), lane = run.
+constexpr int kTileSide = 64;
+struct TileMatrixDev {
+  int tiles_x, ntiles;
+  const int* group_first;   // [ntiles + 1] first group of each tile
+  const int* gray;          // [groups * 32] ray of each lane, -1 if empty
+  const uint16_t* glp;      // [groups * 32] first pixel, tile-local (y*64 + x)
+  const uint16_t* glen;     // [groups * 32] run length (segments)
+  const int* gsteps;        // [groups] longest run of the group
+  const int64_t* gseg_off;  // [groups] entry offset of the group's lengths
+  const int64_t* gcode_off; // [groups] word offset of the step codes
+  const void* tlen;         // lengths, entry (group, step/8, lane, step%8)
+  const uint32_t* tcode;    // 8 x 4-bit step codes per word per lane
+};
+
 // Which per-ray value the forward kernel stores.
 enum FwdOut { FWD_SIRT = 0, FWD_RATIO = 1, FWD_SIM = 2 };
 // What the backward kernel does with its per-pixel sums.
@@ -106,6 +122,29 @@ void launch_weights64(const DevGeom& G, const MatrixDev& M, double* W,
 void launch_convert(const float* in, double* out, int64_t n, cudaStream_t st);
 void launch_narrow(const double* in, float* out, int64_t n, cudaStream_t st);
 void launch_fill64(double* p, int64_t n, double v, cudaStream_t st);
+// tg_tiles.cu
+void launch_runs_count(const DevGeom& G, int tiles_x, int* ray_nruns,
+                       cudaStream_t st);
+void launch_runs_emit(const DevGeom& G, int tiles_x, const int64_t* ray_run_off,
+                      unsigned long long* key, int* val, uint16_t* run_lp,
+                      uint16_t* run_len, int* tile_count, cudaStream_t st);
+int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
+              int* val_in, int* val_out, int64_t n, int tile_bits,
+              cudaStream_t st);
+void launch_runs_group(const unsigned long long* skey, const int* sval,
+                       int64_t nruns, const int* tile_first_run,
+                       const int* group_first, const uint16_t* run_lp,
+                       const uint16_t* run_len, int* gray, uint16_t* glp,
+                       uint16_t* glen, int* gsteps, int* run_slot,
+                       cudaStream_t st);
+void launch_runs_fill(const DevGeom& G, int tiles_x, int len_kind, float scale,
+                      const int64_t* ray_run_off, const int* run_slot,
+                      const int64_t* gseg_off, const int64_t* gcode_off,
+                      void* tlen, uint32_t* tcode, cudaStream_t st);
+void launch_forward_tiled(const IterArgs& A, const TileMatrixDev& T,
+                          const float* recon_batch, float* sim, cudaStream_t st);
+void launch_fwd_finish(const IterArgs& A, float* sim, const float* sino,
+                       float* out, int out_mode, cudaStream_t st);
 // tg_iter.cu
 void launch_fg(const IterArgs& A, const float* recon, const float* W, float* F,
                float* Gv, cudaStream_t st);

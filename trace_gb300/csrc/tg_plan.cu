@@ -34,6 +34,10 @@ struct tg_plan {
   float* d_ra2 = nullptr;
   void* d_dlen = nullptr;
   float* d_W = nullptr;
+  // tile-staged forward (fast mode): the tile-ordered matrix + ray sums
+  bool tiles = false;
+  TileMatrixDev T{};
+  float* d_sim = nullptr;
   // FP64 mode: double state, factors, total lengths and SIRT's a2
   bool fp64 = false;
   double *d_ra2d = nullptr, *d_W64 = nullptr;
@@ -264,6 +268,133 @@ float* batch_ptr(tg_plan* p, float* base, int batch_slot) {
   return base + (int64_t)(batch_slot / p->K) * p->g2 * p->K;
 }
 
+// Tile-ordered forward matrix (tg_tiles.cu): runs of each ray inside 64x64
+// tiles, sorted by (tile, ray) and packed 32 per warp group.
+int build_tiles(tg_plan* p) {
+  const DevGeom& G = p->G;
+  const int C = p->C;
+  const int tiles_x = (C + kTileSide - 1) / kTileSide;
+  const int ntiles = tiles_x * tiles_x;
+  int tile_bits = 1;
+  while ((1 << tile_bits) < ntiles) ++tile_bits;
+  // temporaries of the construction, freed at the end
+  std::vector<std::pair<void*, size_t>> tmp;
+  auto talloc = [&](auto** ptr, size_t n, bool zero) -> int {
+    int rc = dalloc(p, ptr, n, zero);
+    if (rc == TG_OK) tmp.push_back({(void*)*ptr, n * sizeof(**ptr)});
+    return rc;
+  };
+  auto release = [&]() {
+    for (auto& t : tmp) dfree(p, t.first, t.second);
+    tmp.clear();
+  };
+  int* ray_nruns = nullptr;
+  int rc = talloc(&ray_nruns, (size_t)p->R, false);
+  if (rc) return release(), rc;
+  launch_runs_count(G, tiles_x, ray_nruns, p->st);
+  std::vector<int> nruns(p->R);
+  cudaMemcpyAsync(nruns.data(), ray_nruns, p->R * 4, cudaMemcpyDeviceToHost, p->st);
+  if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run count failed");
+  std::vector<int64_t> run_off(p->R);
+  int64_t NR = 0;
+  for (int64_t r = 0; r < p->R; ++r) {
+    run_off[r] = NR;
+    NR += nruns[r];
+  }
+  if (NR > 0x7fffffff) return release(), fail(p, TG_E_GEOMETRY, "too many tile runs");
+  int64_t* d_run_off;
+  unsigned long long *key, *key2;
+  int *val, *val2, *tile_count, *run_slot;
+  uint16_t *run_lp, *run_len;
+  if ((rc = talloc(&d_run_off, (size_t)p->R, false)) || (rc = talloc(&key, (size_t)NR, false)) ||
+      (rc = talloc(&key2, (size_t)NR, false)) || (rc = talloc(&val, (size_t)NR, false)) ||
+      (rc = talloc(&val2, (size_t)NR, false)) || (rc = talloc(&run_lp, (size_t)NR, false)) ||
+      (rc = talloc(&run_len, (size_t)NR, false)) || (rc = talloc(&run_slot, (size_t)NR, false)) ||
+      (rc = talloc(&tile_count, (size_t)ntiles, true)))
+    return release(), rc;
+  cudaMemcpyAsync(d_run_off, run_off.data(), p->R * 8, cudaMemcpyHostToDevice, p->st);
+  launch_runs_emit(G, tiles_x, d_run_off, key, val, run_lp, run_len, tile_count, p->st);
+  if (sort_runs(key, key2, val, val2, NR, tile_bits, p->st))
+    return release(), fail(p, TG_E_CUDA, "sorting the tile runs failed");
+  std::vector<int> tcount(ntiles);
+  cudaMemcpyAsync(tcount.data(), tile_count, ntiles * 4, cudaMemcpyDeviceToHost, p->st);
+  if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run emit failed");
+  std::vector<int> tile_first(ntiles + 1), group_first(ntiles + 1);
+  int runs = 0, groups = 0;
+  for (int t = 0; t < ntiles; ++t) {
+    tile_first[t] = runs;
+    group_first[t] = groups;
+    runs += tcount[t];
+    groups += (tcount[t] + 31) / 32;
+  }
+  tile_first[ntiles] = runs;
+  group_first[ntiles] = groups;
+  int *d_tile_first, *d_group_first, *gray, *gsteps;
+  uint16_t *glp, *glen;
+  if ((rc = talloc(&d_tile_first, (size_t)ntiles + 1, false)) ||
+      (rc = dalloc(p, &d_group_first, (size_t)ntiles + 1)) ||
+      (rc = dalloc(p, &gray, (size_t)groups * 32)) ||
+      (rc = dalloc(p, &glp, (size_t)groups * 32, true)) ||
+      (rc = dalloc(p, &glen, (size_t)groups * 32, true)) ||
+      (rc = dalloc(p, &gsteps, (size_t)groups, true)))
+    return release(), rc;
+  cudaMemsetAsync(gray, 0xff, (size_t)groups * 32 * 4, p->st);  // empty lanes: -1
+  cudaMemcpyAsync(d_tile_first, tile_first.data(), (ntiles + 1) * 4, cudaMemcpyHostToDevice, p->st);
+  cudaMemcpyAsync(d_group_first, group_first.data(), (ntiles + 1) * 4, cudaMemcpyHostToDevice, p->st);
+  launch_runs_group(key2, val2, NR, d_tile_first, d_group_first, run_lp, run_len, gray,
+                    glp, glen, gsteps, run_slot, p->st);
+  std::vector<int> steps(groups);
+  cudaMemcpyAsync(steps.data(), gsteps, (size_t)groups * 4, cudaMemcpyDeviceToHost, p->st);
+  if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run grouping failed");
+  std::vector<int64_t> seg_off(groups), code_off(groups);
+  int64_t entries = 0, words = 0;
+  for (int gi = 0; gi < groups; ++gi) {
+    seg_off[gi] = entries;
+    code_off[gi] = words;
+    entries += (int64_t)((steps[gi] + 7) / 8) * 256;  // chunks of 8 steps
+    words += (int64_t)((steps[gi] + 7) / 8) * 32;
+  }
+  const bool l16 = p->len_kind != TG_LEN_F32;
+  int64_t *d_seg_off, *d_code_off;
+  uint32_t* tcode;
+  void* tlen = nullptr;
+  if ((rc = dalloc(p, &d_seg_off, (size_t)groups)) || (rc = dalloc(p, &d_code_off, (size_t)groups)) ||
+      (rc = dalloc(p, &tcode, (size_t)words, true)))
+    return release(), rc;
+  if (l16) {
+    uint16_t* t;
+    if ((rc = dalloc(p, &t, (size_t)entries, true))) return release(), rc;
+    tlen = t;
+  } else {
+    float* t;
+    if ((rc = dalloc(p, &t, (size_t)entries, true))) return release(), rc;
+    tlen = t;
+  }
+  cudaMemcpyAsync(d_seg_off, seg_off.data(), groups * 8, cudaMemcpyHostToDevice, p->st);
+  cudaMemcpyAsync(d_code_off, code_off.data(), groups * 8, cudaMemcpyHostToDevice, p->st);
+  launch_runs_fill(G, tiles_x, p->len_kind, p->M.scale, d_run_off, run_slot, d_seg_off,
+                   d_code_off, tlen, tcode, p->st);
+  if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run fill failed");
+  release();
+  if ((rc = dalloc(p, &p->d_sim, (size_t)p->R * p->K, true))) return rc;
+  TileMatrixDev& T = p->T;
+  T.tiles_x = tiles_x;
+  T.ntiles = ntiles;
+  T.group_first = d_group_first;
+  T.gray = gray;
+  T.glp = glp;
+  T.glen = glen;
+  T.gsteps = gsteps;
+  T.gseg_off = d_seg_off;
+  T.gcode_off = d_code_off;
+  T.tlen = tlen;
+  T.tcode = tcode;
+  p->tiles = true;
+  p->info.tile_runs = NR;
+  p->info.tile_bytes = entries * (l16 ? 2 : 4) + words * 4 + (int64_t)groups * (32 * 8 + 20);
+  return TG_OK;
+}
+
 int ensure_upd(tg_plan* p) {
   if (p->d_upd) return TG_OK;
   return dalloc(p, &p->d_upd, (size_t)p->R * p->K * (p->fp64 ? 2 : 1));
@@ -311,6 +442,8 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     return fail(nullptr, TG_E_ARG, "unknown len_storage");
   if (d.mode != TG_MODE_EXACT && d.mode != TG_MODE_FAST && d.mode != TG_MODE_FP64)
     return fail(nullptr, TG_E_ARG, "unknown mode");
+  if (d.forward_tiles && d.mode != TG_MODE_FAST)
+    return fail(nullptr, TG_E_ARG, "forward_tiles needs fast mode");
   if (d.mode == TG_MODE_FP64 &&
       (d.len_storage != TG_LEN_F32 || d.slices_per_pass != 1 || d.delta_index))
     return fail(nullptr, TG_E_ARG,
@@ -509,6 +642,12 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
              "4-bit step code; geometry not supported by this layout";
     return bail(TG_E_GEOMETRY);
   }
+  if (d.forward_tiles && (rc = build_tiles(p))) {
+    if (p->err.empty()) p->err = "building the tile-ordered forward matrix failed";
+    return bail(rc);
+  }
+  cudaEventRecord(e1, p->st);
+  cudaEventSynchronize(e1);
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
@@ -724,7 +863,18 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
   }
   for (int it = 0; it < n_iter; ++it) {
     for (int b = 0; b < p->nb; ++b) {
-      run_forward(p, A, b, mode, p->d_upd);
+      if (p->tiles) {
+        const float* src = batch_ptr(p, p->d_recon[p->cur], b * p->K + p->fshift);
+        {
+          Timed t(p, 0);
+          launch_forward_tiled(A, p->T, src, p->d_sim, p->st);
+        }
+        Timed t(p, 2);
+        launch_fwd_finish(A, p->d_sim, p->d_sino + (int64_t)b * p->R * p->K,
+                          p->d_upd, mode, p->st);
+      } else {
+        run_forward(p, A, b, mode, p->d_upd);
+      }
       Timed t(p, 1);
       launch_backward(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
                       p->d_upd, nullptr, EPI_UPDATE, p->st);

@@ -1,0 +1,458 @@
+// Tile-staged forward projection (fast mode).
+//
+// The ray-major forward kernel gathers each segment's K reconstruction values
+// through L1/L2: ~1 sector lookup per segment, and at 2048^2 with 8 slices
+// the 134 MB batch no longer stays in L2 next to the streamed matrix. Here
+// the image is cut into 64 x 64 tiles and each ray's segment list into runs
+// (consecutive segments inside one tile). One block per tile loads the
+// tile's K-slice reconstruction into shared memory once and walks all runs
+// through it: lane = run, 32 runs of adjacent rays per warp. A lane's
+// lengths are stored in chunks of 8 consecutive steps (one 16-byte load per
+// 8 segments for 16-bit codes) with one word of 4-bit step codes per chunk,
+// chunks interleaved across the 32 lanes so each chunk load of a warp is one
+// contiguous 512-byte row; the next chunk is loaded while the current one is
+// consumed. A run's partial sum is added to its ray's sum with
+// one vector reduction; tg::launch_fwd_finish turns the sums into the
+// per-ray factors the backprojection reads and clears them for the next
+// batch. Summation order across runs is not fixed, so this path is used in
+// fast mode only.
+//
+// Construction (once per geometry): count runs per ray, emit run records
+// keyed by (tile, ray, ordinal), radix-sort them (CUB), pack each tile's
+// runs into 32-lane groups, then trace again to fill the groups' streams.
+#include <cub/device/device_radix_sort.cuh>
+
+#include "tg_kernels.cuh"
+
+namespace tg {
+
+namespace {
+
+constexpr int TS = kTileSide;     // tile side (pixels)
+constexpr int RS = TS + 1;        // shared-memory row stride (bank spread)
+constexpr int kBlock = 1024;      // forward: 32 warps per tile
+constexpr int kTraceBlock = 128;
+
+__device__ __forceinline__ int tile_of(const DevGeom& G, int ix, int iy,
+                                       int tiles_x) {
+  return (iy / TS) * tiles_x + ix / TS;
+}
+
+// ---- construction --------------------------------------------------------------
+__global__ void __launch_bounds__(kTraceBlock)
+    k_runs_count(DevGeom G, int tiles_x, int* ray_nruns) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= (int64_t)G.P * G.C) return;
+  const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
+  int n = 0, cur = -1;
+  const int g = G.C;
+  trace_ray(G, a, c, [&](int idx, float, float) {
+    const int t = tile_of(G, idx % g, idx / g, tiles_x);
+    if (t != cur) {
+      ++n;
+      cur = t;
+    }
+  });
+  ray_nruns[r] = n;
+}
+
+__global__ void __launch_bounds__(kTraceBlock)
+    k_runs_emit(DevGeom G, int tiles_x, const int64_t* ray_run_off,
+                unsigned long long* key, int* val, uint16_t* run_lp,
+                uint16_t* run_len, int* tile_count) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= (int64_t)G.P * G.C) return;
+  const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
+  const int g = G.C;
+  int64_t i = ray_run_off[r] - 1;
+  int cur = -1, k = -1, len = 0;
+  auto close = [&]() {
+    if (i >= ray_run_off[r]) run_len[i] = (uint16_t)len;
+  };
+  trace_ray(G, a, c, [&](int idx, float, float) {
+    const int ix = idx % g, iy = idx / g;
+    const int t = tile_of(G, ix, iy, tiles_x);
+    if (t != cur) {
+      close();
+      ++i;
+      ++k;
+      cur = t;
+      len = 0;
+      key[i] = ((unsigned long long)t << 40) | ((unsigned long long)r << 8) |
+               (unsigned long long)(k & 255);
+      val[i] = (int)i;
+      run_lp[i] = (uint16_t)((iy % TS) * TS + ix % TS);
+      atomicAdd(&tile_count[t], 1);
+    }
+    ++len;
+  });
+  close();
+}
+
+__global__ void k_runs_group(const unsigned long long* skey, const int* sval,
+                             int64_t nruns, const int* tile_first_run,
+                             const int* group_first, const uint16_t* run_lp,
+                             const uint16_t* run_len, int* gray, uint16_t* glp,
+                             uint16_t* glen, int* gsteps, int* run_slot) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nruns) return;
+  const unsigned long long k = skey[j];
+  const int t = (int)(k >> 40);
+  const int rank = (int)(j - tile_first_run[t]);
+  const int grp = group_first[t] + rank / 32;
+  const int lane = rank % 32;
+  const int i = sval[j];
+  const int slot = grp * 32 + lane;
+  gray[slot] = (int)((k >> 8) & 0xffffffffull);
+  glp[slot] = run_lp[i];
+  glen[slot] = run_len[i];
+  run_slot[i] = slot;
+  atomicMax(&gsteps[grp], (int)run_len[i]);
+}
+
+template <bool L16>
+__global__ void __launch_bounds__(kTraceBlock)
+    k_runs_fill(DevGeom G, int tiles_x, int len_kind, float scale,
+                const int64_t* ray_run_off, const int* run_slot,
+                const int64_t* gseg_off, const int64_t* gcode_off, void* tlen,
+                uint32_t* tcode) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= (int64_t)G.P * G.C) return;
+  const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
+  const int g = G.C;
+  int64_t i = ray_run_off[r] - 1;
+  int cur = -1, s = 0, px = 0, py = 0;
+  int64_t lbase = 0, cbase = 0;
+  uint32_t word = 0;
+  auto flush = [&]() {
+    if (i >= ray_run_off[r] && (s & 7) != 0) tcode[cbase + (int64_t)(s >> 3) * 32] = word;
+  };
+  trace_ray(G, a, c, [&](int idx, float l, float) {
+    const int ix = idx % g, iy = idx / g;
+    const int t = tile_of(G, ix, iy, tiles_x);
+    if (t != cur) {
+      flush();
+      ++i;
+      cur = t;
+      s = 0;
+      word = 0;
+      const int slot = run_slot[i];
+      const int grp = slot >> 5, lane = slot & 31;
+      lbase = gseg_off[grp] + lane * 8;
+      cbase = gcode_off[grp] + lane;
+    } else {
+      word |= (uint32_t)((ix - px) | ((iy - py + 1) << 1)) << (4 * (s & 7));
+    }
+    // entry (chunk s/8, lane, s%8): chunks of 8 steps, 32 lanes per chunk
+    const int64_t e = lbase + (int64_t)(s >> 3) * 256 + (s & 7);
+    if (L16)
+      reinterpret_cast<uint16_t*>(tlen)[e] = encode16(l, len_kind, scale);
+    else
+      reinterpret_cast<float*>(tlen)[e] = l;
+    if ((s & 7) == 7) {
+      tcode[cbase + (int64_t)(s >> 3) * 32] = word;
+      word = 0;
+    }
+    px = ix;
+    py = iy;
+    ++s;
+  });
+  flush();
+}
+
+// ---- forward -------------------------------------------------------------------
+// Shared-memory image of one tile: K floats per pixel as K/4 float4 planes
+// (K >= 4) or one float/float2 plane, row stride RS pixels.
+template <int K>
+struct TilePlanes {
+  static constexpr int kPlanes = K >= 4 ? K / 4 : 1;
+  static constexpr int kWidth = K >= 4 ? 4 : K;  // floats per plane entry
+  static constexpr int kBytes = TS * RS * K * 4;
+};
+
+template <int K>
+__device__ __forceinline__ void tile_load(float* sm, const float* __restrict__ recon,
+                                          int g, int x0, int y0) {
+  constexpr int W = TilePlanes<K>::kWidth;
+  constexpr int NP = TilePlanes<K>::kPlanes;
+  for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) {
+    const int lx = e % TS, ly = e / TS;
+    const int x = x0 + lx, y = y0 + ly;
+    const int si = ly * RS + lx;
+    const bool in = x < g && y < g;
+    const float* src = recon + ((int64_t)y * g + x) * K;
+#pragma unroll
+    for (int pl = 0; pl < NP; ++pl) {
+      float* dst = sm + ((size_t)pl * TS * RS + si) * W;
+      if constexpr (W == 4) {
+        *reinterpret_cast<float4*>(dst) =
+            in ? __ldg(reinterpret_cast<const float4*>(src) + pl)
+               : make_float4(0.f, 0.f, 0.f, 0.f);
+      } else if constexpr (W == 2) {
+        *reinterpret_cast<float2*>(dst) =
+            in ? __ldg(reinterpret_cast<const float2*>(src)) : make_float2(0.f, 0.f);
+      } else {
+        *dst = in ? __ldg(src) : 0.f;
+      }
+    }
+  }
+}
+
+template <int K>
+__device__ __forceinline__ void tile_fma(const float* sm, int si, float l,
+                                         float (&acc)[K]) {
+  constexpr int W = TilePlanes<K>::kWidth;
+  constexpr int NP = TilePlanes<K>::kPlanes;
+#pragma unroll
+  for (int pl = 0; pl < NP; ++pl) {
+    const float* src = sm + ((size_t)pl * TS * RS + si) * W;
+    if constexpr (W == 4) {
+      const float4 v = *reinterpret_cast<const float4*>(src);
+      acc[pl * 4 + 0] = fmaf(v.x, l, acc[pl * 4 + 0]);
+      acc[pl * 4 + 1] = fmaf(v.y, l, acc[pl * 4 + 1]);
+      acc[pl * 4 + 2] = fmaf(v.z, l, acc[pl * 4 + 2]);
+      acc[pl * 4 + 3] = fmaf(v.w, l, acc[pl * 4 + 3]);
+    } else if constexpr (W == 2) {
+      const float2 v = *reinterpret_cast<const float2*>(src);
+      acc[0] = fmaf(v.x, l, acc[0]);
+      acc[1] = fmaf(v.y, l, acc[1]);
+    } else {
+      acc[0] = fmaf(*src, l, acc[0]);
+    }
+  }
+}
+
+template <int K>
+__device__ __forceinline__ void red_add(float* dst, const float (&acc)[K]) {
+#pragma unroll
+  for (int j = 0; j < K; j += 4) {
+    if constexpr (K >= 4) {
+      asm volatile("red.global.add.v4.f32 [%0], {%1,%2,%3,%4};" ::"l"(dst + j),
+                   "f"(acc[j]), "f"(acc[j + 1]), "f"(acc[j + 2]), "f"(acc[j + 3])
+                   : "memory");
+    }
+  }
+  if constexpr (K == 2) {
+    asm volatile("red.global.add.v2.f32 [%0], {%1,%2};" ::"l"(dst), "f"(acc[0]),
+                 "f"(acc[1])
+                 : "memory");
+  } else if constexpr (K == 1) {
+    atomicAdd(dst, acc[0]);
+  }
+}
+
+// One chunk (8 steps) of a lane's run: lengths + step codes.
+template <int LK>
+struct Chunk {
+  uint4 len[LK == LK_F32 ? 2 : 1];
+  uint32_t code;
+};
+
+template <int LK>
+__device__ __forceinline__ void load_chunk(const TileMatrixDev& T, int64_t lb,
+                                           int64_t cb, int c, Chunk<LK>& ch) {
+  if constexpr (LK == LK_F32) {
+    const uint4* p = reinterpret_cast<const uint4*>(
+        reinterpret_cast<const float*>(T.tlen) + lb + (int64_t)c * 256);
+    ch.len[0] = __ldcs(p);
+    ch.len[1] = __ldcs(p + 1);
+  } else {
+    ch.len[0] = __ldcs(reinterpret_cast<const uint4*>(
+        reinterpret_cast<const uint16_t*>(T.tlen) + lb + (int64_t)c * 256));
+  }
+  ch.code = __ldcs(T.tcode + cb + (int64_t)c * 32);
+}
+
+template <int LK>
+__device__ __forceinline__ float chunk_len(const Chunk<LK>& ch, int j,
+                                           float inv_scale) {
+  if constexpr (LK == LK_F32) {
+    const uint4 q = ch.len[j >> 2];
+    const uint32_t w = (j & 3) == 0 ? q.x : (j & 3) == 1 ? q.y : (j & 3) == 2 ? q.z : q.w;
+    return __uint_as_float(w);
+  } else {
+    const uint4 q = ch.len[0];
+    const uint32_t w = (j >> 1) == 0 ? q.x : (j >> 1) == 1 ? q.y : (j >> 1) == 2 ? q.z : q.w;
+    return decode_len<LK>((uint16_t)((j & 1) ? (w >> 16) : (w & 0xffffu)), inv_scale);
+  }
+}
+
+template <int K, int LK>
+__global__ void __launch_bounds__(kBlock)
+    k_forward_tiled(TileMatrixDev T, int g, float inv_scale,
+                    const float* __restrict__ recon, float* __restrict__ sim) {
+  extern __shared__ float4 smem4[];
+  float* sm = reinterpret_cast<float*>(smem4);
+  const int t = blockIdx.x;
+  const int x0 = (t % T.tiles_x) * TS, y0 = (t / T.tiles_x) * TS;
+  tile_load<K>(sm, recon, g, x0, y0);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g0 = T.group_first[t], g1 = T.group_first[t + 1];
+  for (int grp = g0 + warp; grp < g1; grp += kBlock / 32) {
+    const int slot = grp * 32 + lane;
+    const int ray = T.gray[slot];
+    const int n = T.glen[slot];
+    const int lp = T.glp[slot];
+    int lx = lp % TS, ly = lp / TS;
+    const int chunks = (T.gsteps[grp] + 7) >> 3;
+    const int64_t lb = T.gseg_off[grp] + lane * 8;
+    const int64_t cb = T.gcode_off[grp] + lane;
+    float acc[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) acc[j] = 0.f;
+    Chunk<LK> cur, nxt;
+    if (chunks > 0) load_chunk<LK>(T, lb, cb, 0, cur);
+    for (int c = 0; c < chunks; ++c) {
+      if (c + 1 < chunks) load_chunk<LK>(T, lb, cb, c + 1, nxt);
+      const int s0 = c * 8;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (s0 + j < n) {
+          if (s0 + j > 0) {
+            const uint32_t code = (cur.code >> (4 * j)) & 15u;
+            lx += (int)(code & 1u);
+            ly += (int)(code >> 1) - 1;
+          }
+          tile_fma<K>(sm, ly * RS + lx, chunk_len<LK>(cur, j, inv_scale), acc);
+        }
+      }
+      cur = nxt;
+    }
+    if (ray >= 0 && n > 0) red_add<K>(sim + (int64_t)ray * K, acc);
+  }
+}
+
+// sums -> per-ray factor (as k_forward's epilogue), then clear the sums
+template <int K>
+__global__ void k_fwd_finish(int64_t nrays, const float* __restrict__ ra2,
+                             float* __restrict__ sim, const float* __restrict__ sino,
+                             float* __restrict__ out, int out_mode) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrays) return;
+  Vec<K> s;
+#pragma unroll
+  for (int j = 0; j < K; ++j) s.v[j] = sim[r * K + j];
+  Vec<K> o;
+  if (out_mode == FWD_SIM) {
+    o = s;
+  } else {
+    const Vec<K> ray = load_vec<K>(sino + r * K);
+    const float a2 = out_mode == FWD_SIRT ? ra2[r] : 1.f;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+      o.v[j] = out_mode == FWD_SIRT ? fdiv(fsub(ray.v[j], s.v[j]), a2)
+                                    : fdiv(ray.v[j], s.v[j]);
+  }
+  store_vec<K>(out + r * K, o);
+  Vec<K> z;
+#pragma unroll
+  for (int j = 0; j < K; ++j) z.v[j] = 0.f;
+  store_vec<K>(sim + r * K, z);
+}
+
+template <int K, int LK>
+void fwd_tiled_launch(const TileMatrixDev& T, int g, float inv_scale,
+                      const float* recon, float* sim, cudaStream_t st) {
+  const int smem = TilePlanes<K>::kBytes;
+  cudaFuncSetAttribute(k_forward_tiled<K, LK>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  k_forward_tiled<K, LK><<<T.ntiles, kBlock, smem, st>>>(T, g, inv_scale, recon, sim);
+}
+
+template <int K>
+void fwd_tiled_kind(const TileMatrixDev& T, int g, int len_kind, float inv_scale,
+                    const float* recon, float* sim, cudaStream_t st) {
+  switch (len_kind) {
+    case LK_F32: fwd_tiled_launch<K, LK_F32>(T, g, inv_scale, recon, sim, st); break;
+    case LK_BF16: fwd_tiled_launch<K, LK_BF16>(T, g, inv_scale, recon, sim, st); break;
+    case LK_F16: fwd_tiled_launch<K, LK_F16>(T, g, inv_scale, recon, sim, st); break;
+    default: fwd_tiled_launch<K, LK_U16>(T, g, inv_scale, recon, sim, st); break;
+  }
+}
+
+inline int blocks_for(int64_t n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+void launch_runs_count(const DevGeom& G, int tiles_x, int* ray_nruns,
+                       cudaStream_t st) {
+  const int64_t R = (int64_t)G.P * G.C;
+  k_runs_count<<<blocks_for(R, kTraceBlock), kTraceBlock, 0, st>>>(G, tiles_x, ray_nruns);
+}
+
+void launch_runs_emit(const DevGeom& G, int tiles_x, const int64_t* ray_run_off,
+                      unsigned long long* key, int* val, uint16_t* run_lp,
+                      uint16_t* run_len, int* tile_count, cudaStream_t st) {
+  const int64_t R = (int64_t)G.P * G.C;
+  k_runs_emit<<<blocks_for(R, kTraceBlock), kTraceBlock, 0, st>>>(
+      G, tiles_x, ray_run_off, key, val, run_lp, run_len, tile_count);
+}
+
+int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
+              int* val_in, int* val_out, int64_t n, int tile_bits,
+              cudaStream_t st) {
+  size_t bytes = 0;
+  if (n > 0x7fffffff) return 3;
+  const int end_bit = 40 + tile_bits;
+  cub::DeviceRadixSort::SortPairs(nullptr, bytes, key_in, key_out, val_in, val_out,
+                                  (int)n, 0, end_bit, st);
+  void* tmp = nullptr;
+  if (cudaMalloc(&tmp, bytes) != cudaSuccess) return 1;
+  cub::DeviceRadixSort::SortPairs(tmp, bytes, key_in, key_out, val_in, val_out,
+                                  (int)n, 0, end_bit, st);
+  cudaStreamSynchronize(st);
+  cudaFree(tmp);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+void launch_runs_group(const unsigned long long* skey, const int* sval,
+                       int64_t nruns, const int* tile_first_run,
+                       const int* group_first, const uint16_t* run_lp,
+                       const uint16_t* run_len, int* gray, uint16_t* glp,
+                       uint16_t* glen, int* gsteps, int* run_slot,
+                       cudaStream_t st) {
+  k_runs_group<<<blocks_for(nruns, 256), 256, 0, st>>>(
+      skey, sval, nruns, tile_first_run, group_first, run_lp, run_len, gray, glp,
+      glen, gsteps, run_slot);
+}
+
+void launch_runs_fill(const DevGeom& G, int tiles_x, int len_kind, float scale,
+                      const int64_t* ray_run_off, const int* run_slot,
+                      const int64_t* gseg_off, const int64_t* gcode_off,
+                      void* tlen, uint32_t* tcode, cudaStream_t st) {
+  const int64_t R = (int64_t)G.P * G.C;
+  if (len_kind != LK_F32)
+    k_runs_fill<true><<<blocks_for(R, kTraceBlock), kTraceBlock, 0, st>>>(
+        G, tiles_x, len_kind, scale, ray_run_off, run_slot, gseg_off, gcode_off,
+        tlen, tcode);
+  else
+    k_runs_fill<false><<<blocks_for(R, kTraceBlock), kTraceBlock, 0, st>>>(
+        G, tiles_x, len_kind, scale, ray_run_off, run_slot, gseg_off, gcode_off,
+        tlen, tcode);
+}
+
+void launch_forward_tiled(const IterArgs& A, const TileMatrixDev& T,
+                          const float* recon_batch, float* sim, cudaStream_t st) {
+  const int g = A.G.C;
+  switch (A.K) {
+    case 1: fwd_tiled_kind<1>(T, g, A.M.len_kind, A.M.inv_scale, recon_batch, sim, st); break;
+    case 2: fwd_tiled_kind<2>(T, g, A.M.len_kind, A.M.inv_scale, recon_batch, sim, st); break;
+    case 4: fwd_tiled_kind<4>(T, g, A.M.len_kind, A.M.inv_scale, recon_batch, sim, st); break;
+    default: fwd_tiled_kind<8>(T, g, A.M.len_kind, A.M.inv_scale, recon_batch, sim, st); break;
+  }
+}
+
+void launch_fwd_finish(const IterArgs& A, float* sim, const float* sino,
+                       float* out, int out_mode, cudaStream_t st) {
+  const int64_t R = (int64_t)A.G.P * A.G.C;
+  const int b = blocks_for(R, 256);
+  switch (A.K) {
+    case 1: k_fwd_finish<1><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode); break;
+    case 2: k_fwd_finish<2><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode); break;
+    case 4: k_fwd_finish<4><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode); break;
+    default: k_fwd_finish<8><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode); break;
+  }
+}
+
+}  // namespace tg
