@@ -25,23 +25,51 @@ constexpr int kWarps = 8;
 constexpr int kBlock = kWarps * 32;
 constexpr int kCoefChunk = 512;  // angles of window coefficients per stage
 
+// Four angles of one lane's backward-matrix entries: 16 bytes for 16-bit
+// codes (two per angle), 32 bytes for floats.
 template <int LK>
-__device__ __forceinline__ void stream_pair(const void* dlen, int64_t e,
-                                            float inv_scale, float& l0,
-                                            float& l1, bool& h0, bool& h1) {
+struct Quad {
+  uint4 w[LK == LK_F32 ? 2 : 1];
+};
+
+template <int LK>
+__device__ __forceinline__ void load_quad(const void* dlen, int64_t pair, Quad<LK>& q) {
   if constexpr (LK == LK_F32) {
-    const float2 v = __ldcs(reinterpret_cast<const float2*>(dlen) + e);
-    l0 = v.x;
-    l1 = v.y;
-    // a stored -0.0f marks a zero-length segment (present, adds 0*factor)
-    h0 = __float_as_uint(v.x) != 0u;
-    h1 = __float_as_uint(v.y) != 0u;
+    const uint4* p = reinterpret_cast<const uint4*>(reinterpret_cast<const float2*>(dlen) + pair);
+    q.w[0] = __ldcs(p);
+    q.w[1] = __ldcs(p + 1);
   } else {
-    const uint32_t w = __ldcs(reinterpret_cast<const uint32_t*>(dlen) + e);
+    q.w[0] = __ldcs(reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(dlen) + pair));
+  }
+}
+
+__device__ __forceinline__ uint32_t pick(const uint4& v, int i) {
+  return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+
+// Lengths of angle j of the quad. SCALED: 16-bit fixed-point codes are
+// returned unscaled (the scale is applied once to the pixel's sums).
+template <int LK, bool SCALED>
+__device__ __forceinline__ void quad_pair(const Quad<LK>& q, int j, float inv_scale,
+                                          float& l0, float& l1, bool& h0, bool& h1) {
+  if constexpr (LK == LK_F32) {
+    const uint32_t a = pick(q.w[j >> 1], (j & 1) * 2), b = pick(q.w[j >> 1], (j & 1) * 2 + 1);
+    // a stored -0.0f marks a zero-length segment (present, adds 0*factor)
+    h0 = a != 0u;
+    h1 = b != 0u;
+    l0 = __uint_as_float(a);
+    l1 = __uint_as_float(b);
+  } else {
+    const uint32_t w = pick(q.w[0], j);
     h0 = (w & 0xffffu) != 0u;
     h1 = (w >> 16) != 0u;
-    l0 = decode_len<LK>((uint16_t)(w & 0xffffu), inv_scale);
-    l1 = decode_len<LK>((uint16_t)(w >> 16), inv_scale);
+    if constexpr (LK == LK_U16 && SCALED) {
+      l0 = u16_to_float(w & 0xffffu);
+      l1 = u16_to_float(w >> 16);
+    } else {
+      l0 = decode_len<LK>((uint16_t)(w & 0xffffu), inv_scale);
+      l1 = decode_len<LK>((uint16_t)(w >> 16), inv_scale);
+    }
   }
 }
 
@@ -88,32 +116,45 @@ __global__ void __launch_bounds__(kBlock, 6)
   float acc[K];
 #pragma unroll
   for (int j = 0; j < K; ++j) acc[j] = 0.f;
-  const int64_t astride = (int64_t)A.M.ntiles * 32;  // entries per angle
-  const int64_t e0 = (int64_t)tile * 32 + lane;
-  for (int a0 = 0; a0 < G.P; a0 += kCoefChunk) {
-    const int na = min(kCoefChunk, G.P - a0);
+  // the fixed-point scale of 16-bit codes is applied once, at the end
+  constexpr bool kScaled = (LK == LK_U16) && !EXACT;
+  const int P4 = A.M.P4;
+  const int64_t qstride = (int64_t)A.M.ntiles * 32 * 4;  // pairs per 4 angles
+  for (int a0 = 0; a0 < P4; a0 += kCoefChunk) {
+    const int na = min(kCoefChunk, P4 - a0);  // a multiple of 4
     __syncthreads();
     for (int i = threadIdx.x; i < na; i += kBlock) s_coef[i] = A.M.wcoef[a0 + i];
     __syncthreads();
     if (!valid) continue;
     const float* ua = upd + (int64_t)a0 * G.C * K;
-    int64_t e = e0 + (int64_t)a0 * astride;
-#pragma unroll 4
-    for (int ai = 0; ai < na; ++ai) {
-      float l0, l1;
-      bool h0, h1;
-      stream_pair<LK>(A.M.dlen, e, A.M.inv_scale, l0, l1, h0, h1);
-      if (h0 | h1) {
-        const int c0 = window_c0(s_coef[ai], xf, yf);
-        const float* ub = ua + (int64_t)c0 * K;
-        if (h0) accumulate<K, EXACT, PEN>(acc, rf, l0, ub);
-        if (h1) accumulate<K, EXACT, PEN>(acc, rf, l1, ub + K);
+    int64_t pair = dense_pair(A.M.ntiles, a0, tile, lane);
+    Quad<LK> q;
+    load_quad<LK>(A.M.dlen, pair, q);
+    for (int a4 = 0; a4 < na; a4 += 4) {
+      Quad<LK> nq;
+      if (a4 + 4 < na) load_quad<LK>(A.M.dlen, pair + qstride, nq);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        float l0, l1;
+        bool h0, h1;
+        quad_pair<LK, kScaled>(q, j, A.M.inv_scale, l0, l1, h0, h1);
+        if (h0 | h1) {
+          const int c0 = window_c0(s_coef[a4 + j], xf, yf);
+          const float* ub = ua + ((int64_t)j * G.C + c0) * K;
+          if (h0) accumulate<K, EXACT, PEN>(acc, rf, l0, ub);
+          if (h1) accumulate<K, EXACT, PEN>(acc, rf, l1, ub + K);
+        }
       }
-      e += astride;
-      ua += (int64_t)G.C * K;
+      q = nq;
+      pair += qstride;
+      ua += (int64_t)4 * G.C * K;
     }
   }
   if (!valid) return;
+  if constexpr (kScaled) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) acc[j] *= A.M.inv_scale;
+  }
   if (PEN && !EXACT) {
     const Vec<K> v = load_vec<K>(fsrc);
 #pragma unroll

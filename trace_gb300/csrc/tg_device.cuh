@@ -119,15 +119,30 @@ __device__ __forceinline__ int trace_ray(const DevGeom& G, int a, int c,
 
 // First detector column of the two-column window that holds every ray
 // crossing pixel (x, y) at angle a:
-//   c0 = ceil(-sin*x + cos*y + D),
+//   c0 = round(v + 1/2) (about floor(v) + 1),  v = -sin*x + cos*y + D,
 //   D  = (g/2 - 1/2)(sin - cos) - (|sin| + |cos|)/2 - 1/4 - off,
 // i.e. the detector coordinate of the pixel centre minus half the pixel's
 // footprint (|sin|+|cos| <= sqrt(2) wide) minus a 1/4-column margin for the
-// reference's float jitter, so at most two columns fall in the window.
-// coef = {-sin, cos, D} per angle (host-computed). Construction and use call
-// this same function, so they agree bit for bit.
+// reference's float jitter: the crossing columns lie strictly inside
+// (v + 0.19, v + 1.78), so {c0, c0 + 1} holds all of them (also when v is
+// an integer and the rounding tie goes either way). coef = {-sin, cos,
+// D + 1/2} per angle (host-computed); the rounding is one add of the exact
+// constant 1.5 * 2^23 (valid for |v| < 2^22) instead of two conversions.
+// Construction and use call this same function, so they agree bit for bit.
 __device__ __forceinline__ int window_c0(float4 coef, float xf, float yf) {
-  return (int)ceilf(__fmaf_rn(coef.y, yf, __fmaf_rn(coef.x, xf, coef.z)));
+  const float v = __fmaf_rn(coef.y, yf, __fmaf_rn(coef.x, xf, coef.z));
+  return __float_as_int(__fadd_rn(v, 12582912.0f)) - 0x4B400000;
+}
+
+// Backward-matrix pair index (two slots) of angle a, tile t, lane l: angles
+// in groups of four per lane, so one 16-byte load brings four angles.
+__device__ __forceinline__ int64_t dense_pair(int ntiles, int a, int t, int l) {
+  return (((int64_t)(a >> 2) * ntiles + t) * 32 + l) * 4 + (a & 3);
+}
+
+// Exact float value of a 16-bit integer (magic-number conversion).
+__device__ __forceinline__ float u16_to_float(uint32_t q) {
+  return __uint_as_float(0x4B000000u | q) - 8388608.0f;
 }
 
 // Backward-matrix position of pixel (x, y): 8x4 pixel tiles, one warp per

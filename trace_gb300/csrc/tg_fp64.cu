@@ -51,7 +51,7 @@ __global__ void k_weights64(DevGeom G, MatrixDev M, double* W) {
   const float2* d = reinterpret_cast<const float2*>(M.dlen);
   double sum = 0.0;
   for (int a = 0; a < G.P; ++a) {
-    const float2 v = d[(int64_t)a * M.ntiles * 32 + t];
+    const float2 v = d[dense_pair(M.ntiles, a, tile, lane)];
     sum = __dadd_rn(__dadd_rn(sum, (double)v.x), (double)v.y);
   }
   W[(int64_t)y * g + x] = sum;
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(kBlock)
   const float xf = (float)x, yf = (float)y;
   double acc = 0.0;
   for (int a = 0; a < G.P; ++a) {
-    const float2 v = __ldcs(d + (int64_t)a * A.M.ntiles * 32 + (int64_t)tile * 32 + lane);
+    const float2 v = __ldcs(d + dense_pair(A.M.ntiles, a, tile, lane));
     const bool h0 = __float_as_uint(v.x) != 0u, h1 = __float_as_uint(v.y) != 0u;
     if (!(h0 | h1)) continue;
     const int c0 = window_c0(A.M.wcoef[a], xf, yf);

@@ -26,8 +26,9 @@ struct MatrixDev {
   // tile t at lane l, dlen[((a*ntiles + t)*32 + l)*2 + slot] is the length of
   // ray (a, window_c0 + slot) through the pixel
   const void* dlen;
-  const float4* wcoef; // [P] window coefficients {-sin, cos, D, 0}
+  const float4* wcoef; // [P4] window coefficients {-sin, cos, D, 0}
   int tiles_x, ntiles;
+  int P4;              // angles rounded up to a multiple of 4 (padding empty)
   const float* W;      // [g*g] total length through each pixel
   int len_kind;        // LenKind
   float scale, inv_scale;

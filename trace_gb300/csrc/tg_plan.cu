@@ -517,19 +517,20 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   G.cosq = p->d_cos;
   G.quad = p->d_quad;
 
-  // window coefficients of the backward matrix: c0 = ceil(-s*x + c*y + D)
-  // (tg::window_c0), D from the pixel-centre offset, half the footprint and
-  // a quarter-column margin
-  std::vector<float4> wc(P);
+  // window coefficients of the backward matrix: c0 = round(-s*x + c*y + D)
+  // (tg::window_c0), D from the pixel-centre offset, half the footprint, a
+  // quarter-column margin and the +1/2 of the rounding
+  const int P4 = (P + 3) / 4 * 4;  // backward matrix: angles in fours
+  std::vector<float4> wc(P4, make_float4(0.f, 0.f, 0.f, 0.f));
   const double off = (1.0 - C) / 2.0 + (double)mov;
   for (int a = 0; a < P; ++a) {
     const double sd = sn[a], cd = cs[a];
     const double D = (C / 2.0 - 0.5) * (sd - cd) -
-                     0.5 * (std::fabs(sd) + std::fabs(cd)) - 0.25 - off;
+                     0.5 * (std::fabs(sd) + std::fabs(cd)) - 0.25 - off + 0.5;
     wc[a] = make_float4(-sn[a], cs[a], (float)D, 0.f);
   }
-  if ((rc = dalloc(p, &p->d_wcoef, P))) return bail(rc);
-  cudaMemcpyAsync(p->d_wcoef, wc.data(), P * sizeof(float4),
+  if ((rc = dalloc(p, &p->d_wcoef, P4))) return bail(rc);
+  cudaMemcpyAsync(p->d_wcoef, wc.data(), P4 * sizeof(float4),
                   cudaMemcpyHostToDevice, p->st);
   const int tiles_x = (C + 7) / 8, tiles_y = (C + 3) / 4;
 
@@ -589,7 +590,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     if ((rc = dalloc(p, &t, (size_t)entries, true))) return bail(rc);
     p->d_rlen = t;
   }
-  const size_t dense_n = (size_t)P * tiles_x * tiles_y * 32 * 2;
+  const size_t dense_n = (size_t)P4 * tiles_x * tiles_y * 32 * 2;
   if (l16) {
     uint16_t* t;
     if ((rc = dalloc(p, &t, dense_n, true))) return bail(rc);
@@ -618,6 +619,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   M.wcoef = p->d_wcoef;
   M.tiles_x = tiles_x;
   M.ntiles = tiles_x * tiles_y;
+  M.P4 = P4;
   M.W = p->d_W;
   M.len_kind = p->len_kind;
   M.scale = maxlen > 0 ? 65535.f / maxlen : 1.f;

@@ -52,7 +52,6 @@ __global__ void __launch_bounds__(kTraceBlock)
   const int64_t r = (int64_t)a * G.C + c;
   const int64_t base = M.roff[grp] + lane;
   const float4 coef = M.wcoef[a];
-  const int64_t abase = (int64_t)a * M.ntiles * 32;
   const int64_t cbase = DELTA ? M.rcoff[grp] + lane : 0;
   float a2 = 0.f;
   double a2d = 0.0;
@@ -95,7 +94,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       // the reference too). The 16-bit fixed-point code has no -0.
       int tile, tl;
       pixel_tile(ix, iy, M.tiles_x, &tile, &tl);
-      const int64_t pos = (abase + (int64_t)tile * 32 + tl) * 2 + slot;
+      const int64_t pos = dense_pair(M.ntiles, a, tile, tl) * 2 + slot;
       if (L16) {
         uint16_t* d = reinterpret_cast<uint16_t*>(dlen);
         const float cur = decode16(d[pos], M.len_kind, M.inv_scale);
@@ -131,7 +130,7 @@ __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W) {
   const int64_t p = (int64_t)y * g + x;
   float sum = 0.f, comp = 0.f;
   for (int a = 0; a < G.P; ++a) {
-    const int64_t pos = ((int64_t)a * M.ntiles * 32 + t) * 2;
+    const int64_t pos = dense_pair(M.ntiles, a, tile, lane) * 2;
     float l0, l1;
     if (L16) {
       const uint32_t w =
