@@ -98,6 +98,9 @@ typedef struct {
                              projection through 64x64 reconstruction tiles
                              staged in shared memory (an extra tile-ordered
                              copy of the forward matrix is built) */
+  int backward_staged;    /* fast mode only: the backprojection stages each
+                             16x16-pixel block's detector windows in shared
+                             memory instead of gathering through L1 */
 } tg_plan_desc;
 
 typedef struct {

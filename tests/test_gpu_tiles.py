@@ -13,7 +13,8 @@ pytestmark = pytest.mark.gpu
 @pytest.mark.parametrize("C,P,S,K", [(100, 60, 5, 1), (128, 90, 4, 2), (130, 70, 6, 4),
                                      (96, 50, 9, 8)])
 @pytest.mark.parametrize("alg", ["sirt", "mlem", "pml", "apmlr"])
-def test_tiled_forward_matches_ray_ordered(C, P, S, K, alg):
+@pytest.mark.parametrize("staged", [False, True])
+def test_tiled_forward_matches_ray_ordered(C, P, S, K, alg, staged):
     th = theta_uniform(P)
     rng = np.random.default_rng(C + K)
     sino = rng.uniform(0.5, 2.0, (P, S, C)).astype(np.float32)
@@ -21,7 +22,8 @@ def test_tiled_forward_matches_ray_ordered(C, P, S, K, alg):
     outs = []
     for tiles in (False, True):
         plan = tg.Plan(P, S, C, th, slices_per_pass=K, mode="fast", len_storage="u16",
-                       delta_index=True, forward_tiles=tiles)
+                       delta_index=True, forward_tiles=tiles,
+                       backward_staged=staged and tiles)
         plan.set_sinogram(sino, apply_abs=alg != "sirt")
         plan.reset_recon(alg)
         plan.iterate(alg, 3, prm)

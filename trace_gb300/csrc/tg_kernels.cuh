@@ -111,6 +111,10 @@ void launch_forward(const IterArgs& A, const float* recon_batch,
 void launch_backward(const IterArgs& A, int batch, const float* recon_cur,
                      float* recon_next, const float* upd, float* rep_num,
                      int epi, cudaStream_t st);
+// tg_backward_staged.cu (fast mode)
+void launch_backward_staged(const IterArgs& A, int batch, const float* recon_cur,
+                            float* recon_next, const float* upd, float* rep_num,
+                            int epi, cudaStream_t st);
 // tg_fp64.cu
 void launch_forward64(const IterArgs& A, const double* ra2d, const double* recon,
                       const float* sino, double* out, int out_mode,

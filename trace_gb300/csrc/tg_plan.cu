@@ -442,8 +442,8 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     return fail(nullptr, TG_E_ARG, "unknown len_storage");
   if (d.mode != TG_MODE_EXACT && d.mode != TG_MODE_FAST && d.mode != TG_MODE_FP64)
     return fail(nullptr, TG_E_ARG, "unknown mode");
-  if (d.forward_tiles && d.mode != TG_MODE_FAST)
-    return fail(nullptr, TG_E_ARG, "forward_tiles needs fast mode");
+  if ((d.forward_tiles || d.backward_staged) && d.mode != TG_MODE_FAST)
+    return fail(nullptr, TG_E_ARG, "forward_tiles and backward_staged need fast mode");
   if (d.mode == TG_MODE_FP64 &&
       (d.len_storage != TG_LEN_F32 || d.slices_per_pass != 1 || d.delta_index))
     return fail(nullptr, TG_E_ARG,
@@ -878,8 +878,12 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
         run_forward(p, A, b, mode, p->d_upd);
       }
       Timed t(p, 1);
-      launch_backward(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
-                      p->d_upd, nullptr, EPI_UPDATE, p->st);
+      if (!p->d.backward_staged)
+        launch_backward(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
+                        p->d_upd, nullptr, EPI_UPDATE, p->st);
+      else
+        launch_backward_staged(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
+                               p->d_upd, nullptr, EPI_UPDATE, p->st);
     }
     p->cur ^= 1;
   }
@@ -899,8 +903,12 @@ int tg_reduce(tg_plan* p, int alg, const tg_params* prm) {
   for (int b = 0; b < p->nb; ++b) {
     run_forward(p, A, b, mode, p->d_upd);
     Timed t(p, 1);
-    launch_backward(A, b, p->d_recon[p->cur], nullptr, p->d_upd, p->d_rep,
-                    EPI_REPLICA, p->st);
+    if (!p->d.backward_staged)
+      launch_backward(A, b, p->d_recon[p->cur], nullptr, p->d_upd, p->d_rep,
+                      EPI_REPLICA, p->st);
+    else
+      launch_backward_staged(A, b, p->d_recon[p->cur], nullptr, p->d_upd,
+                             p->d_rep, EPI_REPLICA, p->st);
   }
   TG_CUDA(p, cudaGetLastError());
   return TG_OK;
