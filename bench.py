@@ -286,11 +286,33 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     prm = tg.default_params("pml", beta=W["beta"])
     K = args.slices_per_pass
     hbm_peak, peak_kind = peaks()
+    t0 = time.time()
+    tuned = None
+    if args.autotune:
+        from trace_gb300.autotune import autotune
+        from trace_gb300.phantom import ellipse_phantoms_torch
+        n = min(16, S)
+        tp = tg.Plan(P, n, C, theta, len_storage=args.len_storage, mode="fast",
+                     delta_index=True)
+        tp.set_stream(stream)
+        tp.set_recon("sirt", ellipse_phantoms_torch(C, n, seed=99, device=dev,
+                                                    texture_sigma=W["texture"]))
+        sample = torch.empty((P, n, C), dtype=torch.float32, device=dev)
+        tp.forward_project("sirt", out=sample)
+        tp.close()
+        best, res = autotune(theta, sample, "pml", prm, len_storage=args.len_storage,
+                             stream=stream)
+        K, args.tiles, args.staged = (best["slices_per_pass"], best["forward_tiles"],
+                                      best["backward_staged"])
+        args.slices_per_pass = K
+        tuned = {"chosen": best, "sample_slices": n,
+                 "ms_per_slice_iter": [[c, round(ms, 4)] for c, ms, _ in res]}
+        del sample
 
     # ---- mixed-precision batched path (the measured value)
-    t0 = time.time()
     plan = tg.Plan(P, S, C, theta, len_storage=args.len_storage, slices_per_pass=K,
-                   mode="fast", delta_index=True, forward_tiles=args.tiles)
+                   mode="fast", delta_index=True, forward_tiles=args.tiles,
+                   backward_staged=args.staged)
     plan.set_stream(stream)
     info = plan.info()
     sino = make_data(W, dev, plan)
@@ -388,7 +410,7 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
         "roofline": roofline, "clocks": clk.summary(), "gpu_launches": launches,
         "setup_ms": info["setup_ms"], "num_segments_per_slice": info["num_segments"],
         "device_bytes": info["device_bytes"],
-        "rel_l2_vs_fp64": rel, "plain_fp32": plain, "e2e": e2e,
+        "rel_l2_vs_fp64": rel, "plain_fp32": plain, "e2e": e2e, "autotune": tuned,
         "cpu_baseline": cpu,
         "wall_s": time.time() - t0,
     }
@@ -406,7 +428,7 @@ def fp64_check(args, W, theta, sino, prm, tg, torch, dev):
     configs = {
         "fp64": dict(len_storage="f32", mode="fp64"),
         "mixed": dict(len_storage=args.len_storage, mode="fast", delta_index=True,
-                      forward_tiles=args.tiles),
+                      forward_tiles=args.tiles, backward_staged=args.staged),
         "plain_fp32": dict(len_storage="f32", mode="exact"),
     }
     runs = {}
@@ -464,7 +486,8 @@ def end_to_end(args, W, theta, sino, prm, tg, torch, stream):
         t = time.perf_counter()
         p = tg.Plan(W["P"], W["S"], W["C"], theta, len_storage=args.len_storage,
                     slices_per_pass=args.slices_per_pass, mode="fast",
-                    delta_index=True, forward_tiles=args.tiles)
+                    delta_index=True, forward_tiles=args.tiles,
+                    backward_staged=args.staged)
         p.set_stream(stream)
         p.set_sinogram(host, apply_abs=True)
         p.reset_recon("pml")
@@ -494,6 +517,11 @@ def main():
     ap.add_argument("--slices-per-pass", type=int, default=8)
     ap.add_argument("--no-tiles", dest="tiles", action="store_false",
                     help="ray-ordered forward projection instead of the tile-staged one")
+    ap.add_argument("--staged", action="store_true",
+                    help="shared-memory-staged backprojection")
+    ap.add_argument("--autotune", action="store_true",
+                    help="time the plan configurations on a 16-slice sample first "
+                         "and run the fastest")
     ap.add_argument("--no-plain", dest="plain", action="store_false")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")

@@ -186,6 +186,28 @@ int tg_reset_replica(tg_plan* plan);
  * per slice batch, n_iter times. */
 int tg_iterate(tg_plan* plan, int alg, const tg_params* params, int n_iter);
 
+/* Capture each fused iteration of tg_iterate in a CUDA graph (one per
+ * reconstruction-buffer parity, re-captured when the algorithm or its
+ * parameters change) and replay it. Needs the plan's own stream or a
+ * user stream other than the legacy default stream; ignored while the
+ * per-kernel timers are on. */
+int tg_plan_set_graphs(tg_plan* plan, int enable);
+
+/* A batch of independent plans (any geometries) iterated together: each
+ * iteration of every plan is captured into one CUDA graph whose branches
+ * run on up to 16 streams, so one graph launch advances all of them - the
+ * counterpart of running many drivers (or MPI ranks over disjoint slice
+ * blocks, trace_h5io.cc:7-22) side by side. Plans must be ready to iterate
+ * (layout, sinogram) and stay owned by the caller. tg_batch_iterate returns
+ * after the work has finished. */
+typedef struct tg_batch tg_batch;
+int tg_batch_create(tg_plan* const* plans, int n, tg_batch** out);
+int tg_batch_iterate(tg_batch* batch, const int* algs, const tg_params* params,
+                     int n_iter);
+int tg_batch_synchronize(tg_batch* batch);
+int tg_batch_destroy(tg_batch* batch);
+const char* tg_batch_last_error(const tg_batch* batch);
+
 /* Forward projection of the current reconstruction: sim [P][S][C]. */
 int tg_forward_project(tg_plan* plan, int alg, const tg_params* params,
                        float* sim, int on_device);

@@ -1,0 +1,60 @@
+"""CUDA-graph replay of iterations and batches of independent plans: the
+results must be bit-identical to plain launches (exact mode)."""
+import numpy as np
+import pytest
+
+import trace_gb300 as tg
+from tests._util import bits, theta_uniform
+
+pytestmark = pytest.mark.gpu
+
+
+def _plan(C, P, S, seed, alg, **kw):
+    rng = np.random.default_rng(seed)
+    sino = rng.uniform(0.5, 2.0, (P, S, C)).astype(np.float32)
+    plan = tg.Plan(P, S, C, theta_uniform(P), **kw)
+    plan.set_sinogram(sino, apply_abs=alg != "sirt")
+    plan.reset_recon(alg)
+    return plan
+
+
+@pytest.mark.parametrize("alg", ["sirt", "pml", "apmlr"])
+@pytest.mark.parametrize("kw", [dict(slices_per_pass=2),
+                                dict(slices_per_pass=4, mode="fast", len_storage="u16",
+                                     delta_index=True, forward_tiles=True)])
+def test_graph_replay_identical(alg, kw):
+    prm = tg.default_params(alg, beta=0.3)
+    outs = []
+    for graphs in (False, True):
+        plan = _plan(64, 48, 5, 1, alg, **kw)
+        plan.set_graphs(graphs)
+        plan.iterate(alg, 3, prm)
+        plan.iterate(alg, 2, prm)  # parity flips between calls
+        outs.append(plan.get_recon(alg))
+        plan.close()
+    if kw.get("forward_tiles"):  # ray sums arrive by atomics: order may vary
+        assert np.max(np.abs(outs[1] - outs[0])) <= 1e-5 * np.max(np.abs(outs[0]))
+    else:
+        assert np.array_equal(bits(outs[0]), bits(outs[1]))
+
+
+def test_batch_matches_individual_plans():
+    specs = [(64, 40, 3, "sirt"), (96, 70, 2, "mlem"), (48, 33, 5, "pml"),
+             (80, 25, 1, "mlem"), (64, 90, 4, "sirt")]
+    prms = [tg.default_params(a, beta=0.4) for *_, a in specs]
+    singles = []
+    for i, (C, P, S, alg) in enumerate(specs):
+        plan = _plan(C, P, S, 10 + i, alg, slices_per_pass=2)
+        plan.iterate(alg, 4, prms[i])
+        singles.append(plan.get_recon(alg))
+        plan.close()
+    plans = [_plan(C, P, S, 10 + i, alg, slices_per_pass=2)
+             for i, (C, P, S, alg) in enumerate(specs)]
+    batch = tg.Batch(plans)
+    batch.iterate([a for *_, a in specs], 3, prms)
+    batch.iterate([a for *_, a in specs], 1, prms)
+    for plan, (C, P, S, alg), want in zip(plans, specs, singles):
+        assert np.array_equal(bits(plan.get_recon(alg)), bits(want))
+    batch.close()
+    for p in plans:
+        p.close()

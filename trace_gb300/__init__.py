@@ -34,7 +34,9 @@ EXPORTED = [
     "tg_get_recon", "tg_reduce", "tg_get_replica", "tg_calculate_fg",
     "tg_get_fg", "tg_update_recon", "tg_reset_replica", "tg_iterate",
     "tg_forward_project", "tg_trace_rays", "tg_plan_set_timing",
-    "tg_plan_get_timing",
+    "tg_plan_get_timing", "tg_plan_set_graphs", "tg_batch_create",
+    "tg_batch_iterate", "tg_batch_synchronize", "tg_batch_destroy",
+    "tg_batch_last_error",
 ]
 
 
@@ -91,6 +93,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.tg_last_error.restype = C.c_char_p
     lib.tg_last_error.argtypes = [vp]
     lib.tg_plan_create.argtypes = [C.POINTER(PlanDesc), vp, vp, vp, C.POINTER(vp)]
+    lib.tg_batch_last_error.restype = C.c_char_p
+    lib.tg_batch_last_error.argtypes = [vp]
     for name in EXPORTED:
         getattr(lib, name)  # every declared symbol must exist
     _lib = lib
@@ -182,6 +186,10 @@ class Plan:
 
     def set_stream(self, stream_ptr):
         self._chk(self._lib.tg_plan_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    def set_graphs(self, enable=True):
+        """Replay each fused iteration from a captured CUDA graph."""
+        self._chk(self._lib.tg_plan_set_graphs(self._h, int(bool(enable))))
 
     def set_timing(self, enable=True):
         self._chk(self._lib.tg_plan_set_timing(self._h, int(bool(enable))))
@@ -287,6 +295,46 @@ class Plan:
         self._chk(self._lib.tg_trace_rays(self._h, _ptr(counts), _ptr(offs), _ptr(idx),
                                           _ptr(ln), _ptr(ln2)))
         return counts, offs, idx, ln, ln2
+
+
+class Batch:
+    """Independent plans advanced together, one CUDA graph launch per
+    iteration (tg_batch_*)."""
+
+    def __init__(self, plans):
+        self._lib = load_library()
+        self.plans = list(plans)
+        arr = (C.c_void_p * len(self.plans))(*[p.handle for p in self.plans])
+        h = C.c_void_p()
+        rc = self._lib.tg_batch_create(arr, len(self.plans), C.byref(h))
+        if rc:
+            raise TraceError(rc, self._lib.tg_batch_last_error(None).decode())
+        self._h = h
+
+    def iterate(self, algs, n_iter=1, params=None):
+        n = len(self.plans)
+        if isinstance(algs, (str, int)):
+            algs = [algs] * n
+        a = (C.c_int * n)(*[ALGS[x] if isinstance(x, str) else int(x) for x in algs])
+        if params is None:
+            params = [default_params(x) for x in algs]
+        elif isinstance(params, Params):
+            params = [params] * n
+        pr = (Params * n)(*params)
+        rc = self._lib.tg_batch_iterate(self._h, a, pr, int(n_iter))
+        if rc:
+            raise TraceError(rc, self._lib.tg_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.tg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def degree_to_radian(theta):

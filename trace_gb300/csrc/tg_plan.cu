@@ -62,6 +62,15 @@ struct tg_plan {
   tg_plan_info info{};
   int64_t dev_bytes = 0;
   std::vector<void*> allocs;
+  // CUDA graphs of one iteration, one per buffer parity, keyed by the
+  // algorithm and parameters they were captured with
+  bool use_graphs = false;
+  struct Graph {
+    bool valid = false;
+    int alg = -1;
+    tg_params prm{};
+    cudaGraphExec_t exec = nullptr;
+  } graphs[2];
   // per-kernel timers: event pairs recorded around launches while enabled
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -201,8 +210,16 @@ int check_layout(tg_plan* p, int alg) {
   return TG_OK;
 }
 
+void drop_graphs(tg_plan* p) {
+  for (auto& g : p->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = tg_plan::Graph();
+  }
+}
+
 int establish_layout(tg_plan* p, int alg) {
   if (!valid_alg(alg)) return fail(p, TG_E_ARG, "unknown algorithm");
+  drop_graphs(p);
   const int halo = halo_of(alg);
   int vshift = 0, fshift = 0;
   if (alg == TG_APMLR) {
@@ -711,6 +728,7 @@ int tg_plan_get_timing(tg_plan* p, tg_timing* out) {
 int tg_plan_destroy(tg_plan* p) {
   if (!p) return TG_OK;
   if (p->st) cudaStreamSynchronize(p->st);
+  drop_graphs(p);
   for (auto& u : p->ev_used) {
     cudaEventDestroy(u.second.first);
     cudaEventDestroy(u.second.second);
@@ -836,12 +854,56 @@ static int run_forward(tg_plan* p, const IterArgs& A, int b, int out_mode,
   return TG_OK;
 }
 
-int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
-  if (!p || n_iter < 0) return p ? fail(p, TG_E_ARG, "bad n_iter") : TG_E_ARG;
+// Launches of one fused iteration on the plan's stream (buffers by p->cur;
+// the caller flips p->cur).
+static void issue_iteration(tg_plan* p, const IterArgs& A, int mode) {
+  for (int b = 0; b < p->nb; ++b) {
+    if (p->tiles) {
+      const float* src = batch_ptr(p, p->d_recon[p->cur], b * p->K + p->fshift);
+      {
+        Timed t(p, 0);
+        launch_forward_tiled(A, p->T, src, p->d_sim, p->st);
+      }
+      Timed t(p, 2);
+      launch_fwd_finish(A, p->d_sim, p->d_sino + (int64_t)b * p->R * p->K,
+                        p->d_upd, mode, p->st);
+    } else {
+      run_forward(p, A, b, mode, p->d_upd);
+    }
+    Timed t(p, 1);
+    if (!p->d.backward_staged)
+      launch_backward(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
+                      p->d_upd, nullptr, EPI_UPDATE, p->st);
+    else
+      launch_backward_staged(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
+                             p->d_upd, nullptr, EPI_UPDATE, p->st);
+  }
+}
+
+// Checks shared by tg_iterate and tg_batch_iterate.
+static int iterate_ready(tg_plan* p, int alg, const tg_params* prm) {
   TG_TRY(check_layout(p, alg));
   if (!p->have_sino) return fail(p, TG_E_STATE, "no sinogram uploaded");
   if (alg >= TG_PML && !prm) return fail(p, TG_E_ARG, "penalised algorithms need params");
-  TG_TRY(ensure_upd(p));
+  return ensure_upd(p);
+}
+
+static bool same_params(const tg_params& a, const tg_params* b) {
+  const tg_params z{};
+  return std::memcmp(&a, b ? b : &z, sizeof(tg_params)) == 0;
+}
+
+int tg_plan_set_graphs(tg_plan* p, int enable) {
+  if (!p) return TG_E_ARG;
+  TG_CUDA(p, cudaStreamSynchronize(p->st));
+  drop_graphs(p);
+  p->use_graphs = enable != 0;
+  return TG_OK;
+}
+
+int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
+  if (!p || n_iter < 0) return p ? fail(p, TG_E_ARG, "bad n_iter") : TG_E_ARG;
+  TG_TRY(iterate_ready(p, alg, prm));
   const IterArgs A = make_args(p, alg, prm);
   const int mode = alg == TG_SIRT ? FWD_SIRT : FWD_RATIO;
   if (p->fp64) {
@@ -863,31 +925,184 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
     TG_CUDA(p, cudaGetLastError());
     return TG_OK;
   }
+  // graphs need a capturable stream and no per-launch timers
+  const bool graphs = p->use_graphs && !p->timing && p->st != nullptr;
   for (int it = 0; it < n_iter; ++it) {
-    for (int b = 0; b < p->nb; ++b) {
-      if (p->tiles) {
-        const float* src = batch_ptr(p, p->d_recon[p->cur], b * p->K + p->fshift);
-        {
-          Timed t(p, 0);
-          launch_forward_tiled(A, p->T, src, p->d_sim, p->st);
-        }
-        Timed t(p, 2);
-        launch_fwd_finish(A, p->d_sim, p->d_sino + (int64_t)b * p->R * p->K,
-                          p->d_upd, mode, p->st);
-      } else {
-        run_forward(p, A, b, mode, p->d_upd);
+    if (graphs) {
+      tg_plan::Graph& g = p->graphs[p->cur];
+      if (!g.valid || g.alg != alg || !same_params(g.prm, prm)) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = tg_plan::Graph();
+        cudaGraph_t graph;
+        TG_CUDA(p, cudaStreamBeginCapture(p->st, cudaStreamCaptureModeThreadLocal));
+        issue_iteration(p, A, mode);
+        TG_CUDA(p, cudaStreamEndCapture(p->st, &graph));
+        const cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(p, TG_E_CUDA, cudaGetErrorString(e));
+        g.valid = true;
+        g.alg = alg;
+        g.prm = prm ? *prm : tg_params{};
       }
-      Timed t(p, 1);
-      if (!p->d.backward_staged)
-        launch_backward(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
-                        p->d_upd, nullptr, EPI_UPDATE, p->st);
-      else
-        launch_backward_staged(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
-                               p->d_upd, nullptr, EPI_UPDATE, p->st);
+      TG_CUDA(p, cudaGraphLaunch(g.exec, p->st));
+    } else {
+      issue_iteration(p, A, mode);
     }
     p->cur ^= 1;
   }
   TG_CUDA(p, cudaGetLastError());
+  return TG_OK;
+}
+
+// ---- batches of plans: one graph launch per iteration for all of them ------
+struct tg_batch {
+  std::vector<tg_plan*> plans;
+  std::vector<cudaStream_t> streams;  // branch streams of the captured graph
+  cudaStream_t main = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  struct Graph {
+    bool valid = false;
+    std::vector<int> algs;
+    std::vector<tg_params> prms;
+    int cur0 = -1;  // plan 0's buffer parity the graph was captured in
+    cudaGraphExec_t exec = nullptr;
+  } graphs[2];
+  std::string err;
+};
+
+extern "C" int tg_batch_create(tg_plan* const* plans, int n, tg_batch** out) {
+  if (!plans || n < 1 || !out) return fail(nullptr, TG_E_ARG, "need plans");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i)
+    if (!plans[i] || plans[i]->fp64)
+      return fail(nullptr, TG_E_ARG, "batch plans must be FP32 plans");
+  tg_batch* b = new (std::nothrow) tg_batch();
+  if (!b) return fail(nullptr, TG_E_NOMEM, "host allocation failed");
+  b->plans.assign(plans, plans + n);
+  const int nstreams = n < 16 ? n : 16;
+  bool ok = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; ok && i < nstreams; ++i) {
+    cudaStream_t s;
+    cudaEvent_t e;
+    ok = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    if (ok) {
+      b->streams.push_back(s);
+      b->joins.push_back(e);
+    }
+  }
+  if (!ok) {
+    g_create_error = "stream/event creation failed";
+    tg_batch_destroy(b);
+    return TG_E_CUDA;
+  }
+  *out = b;
+  return TG_OK;
+}
+
+extern "C" int tg_batch_destroy(tg_batch* b) {
+  if (!b) return TG_OK;
+  if (b->main) cudaStreamSynchronize(b->main);
+  for (auto& g : b->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  for (auto s : b->streams) cudaStreamDestroy(s);
+  for (auto e : b->joins) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->main) cudaStreamDestroy(b->main);
+  delete b;
+  return TG_OK;
+}
+
+extern "C" const char* tg_batch_last_error(const tg_batch* b) {
+  return b ? b->err.c_str() : g_create_error.c_str();
+}
+
+extern "C" int tg_batch_synchronize(tg_batch* b) {
+  if (!b) return TG_E_ARG;
+  const cudaError_t e = cudaStreamSynchronize(b->main);
+  if (e != cudaSuccess) {
+    b->err = cudaGetErrorString(e);
+    return TG_E_CUDA;
+  }
+  return TG_OK;
+}
+
+extern "C" int tg_batch_iterate(tg_batch* b, const int* algs, const tg_params* params,
+                                int n_iter) {
+  if (!b || !algs || n_iter < 0) return TG_E_ARG;
+  const int n = (int)b->plans.size();
+  for (int i = 0; i < n; ++i) {
+    tg_plan* p = b->plans[i];
+    const int rc = iterate_ready(p, algs[i], params ? &params[i] : nullptr);
+    if (rc) {
+      b->err = "plan " + std::to_string(i) + ": " + p->err;
+      return rc;
+    }
+    if (p->timing) {
+      b->err = "plan " + std::to_string(i) + " has per-kernel timers on";
+      return TG_E_STATE;
+    }
+  }
+  // plans' own streams must be done before the graph (on `main`) reads their data
+  for (tg_plan* p : b->plans) cudaStreamSynchronize(p->st);
+  for (int it = 0; it < n_iter; ++it) {
+    const int parity = b->plans[0]->cur;
+    tg_batch::Graph& g = b->graphs[parity];
+    bool match = g.valid && g.cur0 == parity;
+    for (int i = 0; match && i < n; ++i)
+      match = g.algs[i] == algs[i] &&
+              same_params(g.prms[i], params ? &params[i] : nullptr);
+    if (!match) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g = tg_batch::Graph();
+      cudaGraph_t graph;
+      cudaError_t e = cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) e = cudaEventRecord(b->fork, b->main);
+      const int ns = (int)b->streams.size();
+      for (int s = 0; e == cudaSuccess && s < ns; ++s)
+        e = cudaStreamWaitEvent(b->streams[s], b->fork, 0);
+      for (int i = 0; e == cudaSuccess && i < n; ++i) {
+        tg_plan* p = b->plans[i];
+        const cudaStream_t keep = p->st;
+        p->st = b->streams[i % ns];
+        const IterArgs A = make_args(p, algs[i], params ? &params[i] : nullptr);
+        issue_iteration(p, A, algs[i] == TG_SIRT ? FWD_SIRT : FWD_RATIO);
+        p->st = keep;
+      }
+      for (int s = 0; e == cudaSuccess && s < ns; ++s) {
+        e = cudaEventRecord(b->joins[s], b->streams[s]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->main, b->joins[s], 0);
+      }
+      const cudaError_t e2 = cudaStreamEndCapture(b->main, &graph);
+      if (e == cudaSuccess) e = e2;
+      if (e == cudaSuccess) {
+        e = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+      }
+      if (e != cudaSuccess) {
+        b->err = std::string("graph capture failed: ") + cudaGetErrorString(e);
+        return TG_E_CUDA;
+      }
+      g.valid = true;
+      g.cur0 = parity;
+      g.algs.assign(algs, algs + n);
+      for (int i = 0; i < n; ++i) g.prms.push_back(params ? params[i] : tg_params{});
+    }
+    const cudaError_t e = cudaGraphLaunch(g.exec, b->main);
+    if (e != cudaSuccess) {
+      b->err = cudaGetErrorString(e);
+      return TG_E_CUDA;
+    }
+    for (tg_plan* p : b->plans) p->cur ^= 1;
+  }
+  // later calls on the plans' own streams see the batch's results
+  const cudaError_t e = cudaStreamSynchronize(b->main);
+  if (e != cudaSuccess) {
+    b->err = cudaGetErrorString(e);
+    return TG_E_CUDA;
+  }
   return TG_OK;
 }
 
