@@ -252,8 +252,31 @@ def time_iterations(plan, alg, prm, n, stream_ptr, torch):
     return ev0.elapsed_time(ev1)
 
 
-def kernel_bytes(info, W, K, tiles, pen=True):
-    """Algorithmic bytes per launch of the forward and backward kernels."""
+LEN_BYTES = {"f32": 4, "bf16": 2, "f16": 2, "u16": 2}
+
+
+def kernel_bytes(info, W, K, len_storage, pen=True):
+    """Algorithmic bytes per launch of the forward and backward kernels.
+
+    The per-unit figure of the cached-segment-list formulation: every pass
+    over one slice geometry's segments moves (4 + L) bytes per segment (int32
+    pixel index + L-byte length) and serves K slices; per slice the forward
+    pass adds the sinogram row read (4 P C) and one reconstruction read
+    (4 g^2), the backprojection the reconstruction read and write (8 g^2)
+    and, for the penalised algorithms, F and G written and read back plus
+    the neighbour reads (12 g^2). Summed over both kernels this is
+    2 Nseg (4 + L) / K + 4 P C + 12 g^2 + 12 g^2 per slice-iteration.
+    """
+    C, P = W["C"], W["P"]
+    g2 = C * C
+    seg = info["num_segments"] * (4 + LEN_BYTES[len_storage])
+    fwd = seg + K * (4 * P * C + 4 * g2)
+    back = seg + K * (8 * g2 + (12 * g2 if pen else 0))
+    return fwd, back
+
+
+def format_bytes(info, W, K, tiles, pen=True):
+    """Bytes the kernels' own compressed matrix formats move per launch."""
     C, P = W["C"], W["P"]
     R, g2 = P * C, C * C
     if tiles:  # tile stream + one read of the batch + the ray sums written
@@ -336,7 +359,8 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     nb = info["batches"]
     launches = args.steps * nb * (3 if args.tiles else 2)
 
-    fwd_b, back_b = kernel_bytes(info, W, K, args.tiles)
+    fwd_b, back_b = kernel_bytes(info, W, K, args.len_storage)
+    fwd_f, back_f = format_bytes(info, W, K, args.tiles)
     fwd_avg = tim["forward_ms"] / max(tim["forward_launches"], 1)
     back_avg = tim["backward_ms"] / max(tim["backward_launches"], 1)
     dom = "backward" if tim["backward_ms"] >= tim["forward_ms"] else "forward"
@@ -345,20 +369,26 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     dom_bytes, dom_ms = (back_b, back_avg) if dom == "backward" else (fwd_b, fwd_avg)
     achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
     traffic = ncu_traffic().get(f"{kname}:{args.workload}:{args.len_storage}:K{K}")
+
+    def gbs(b, ms):
+        return b / (ms / 1e3) / 1e9 if ms else None
+
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
         "frac": achieved / hbm_peak, "peak_kind": f"{peak_kind} (burst copy)",
         "traffic": traffic, "kernel": kname,
         "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": dom_ms,
+        "bytes_definition": "segments x (4 + L) per matrix pass + per-slice "
+                            "sinogram/reconstruction/penalty bytes x K",
         "share": (tim["backward_ms"] if dom == "backward" else tim["forward_ms"]) /
                  max(tim["forward_ms"] + tim["backward_ms"], 1e-9),
         "kernels": {
             ("k_forward_tiled" if args.tiles else "k_forward"): {
-                "avg_ms": fwd_avg, "bytes": fwd_b,
-                "gbs": fwd_b / (fwd_avg / 1e3) / 1e9 if fwd_avg else None},
+                "avg_ms": fwd_avg, "bytes": fwd_b, "gbs": gbs(fwd_b, fwd_avg),
+                "format_bytes": fwd_f, "format_gbs": gbs(fwd_f, fwd_avg)},
             "k_fwd_finish": {"avg_ms": tim["other_ms"] / max(tim["other_launches"], 1)},
-            "k_backward": {"avg_ms": back_avg, "bytes": back_b,
-                           "gbs": back_b / (back_avg / 1e3) / 1e9 if back_avg else None},
+            "k_backward": {"avg_ms": back_avg, "bytes": back_b, "gbs": gbs(back_b, back_avg),
+                           "format_bytes": back_f, "format_gbs": gbs(back_f, back_avg)},
         },
     }
 
