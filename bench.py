@@ -9,8 +9,10 @@ Gaussian texture (sigma 0.02), projected by the plan's own projector, |x|
 applied on upload as the PML driver does (pml_main.cc:122).
 
 Arms
-  ours (default)  the mixed-precision batched path: 16-bit lengths, 8 slices
-                  per matrix pass, fused backprojection+update. A "step" is one
+  ours (default)  the mixed-precision batched path: 16-bit lengths, 16-bit
+                  gather operands (reconstruction tile, factors - 1), FP32
+                  arithmetic, 8 slices per matrix pass, fused
+                  backprojection+update. A "step" is one
                   iteration over all 128 slices; `value` = slice-iterations/s
                   with inputs resident on the device. Also reported: the plain
                   FP32 path (f32 lengths, one slice per pass, reference op
@@ -335,7 +337,7 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     # ---- mixed-precision batched path (the measured value)
     plan = tg.Plan(P, S, C, theta, len_storage=args.len_storage, slices_per_pass=K,
                    mode="fast", delta_index=True, forward_tiles=args.tiles,
-                   backward_staged=args.staged)
+                   backward_staged=args.staged, half_gathers=args.half)
     plan.set_stream(stream)
     info = plan.info()
     sino = make_data(W, dev, plan)
@@ -430,6 +432,7 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
                 "projected by the plan's projector",
         "config": {"workload": W["name"], "slices_per_pass": K,
                    "len_storage": args.len_storage, "index": "4-bit delta",
+                   "gather_operands": "f16 (tile, factor-1)" if args.half else "f32",
                    "forward": "tile-staged (64x64 shared-memory tiles)" if args.tiles
                               else "ray-ordered",
                    "step": f"one PML iteration over all {S} slices",
@@ -458,7 +461,8 @@ def fp64_check(args, W, theta, sino, prm, tg, torch, dev):
     configs = {
         "fp64": dict(len_storage="f32", mode="fp64"),
         "mixed": dict(len_storage=args.len_storage, mode="fast", delta_index=True,
-                      forward_tiles=args.tiles, backward_staged=args.staged),
+                      forward_tiles=args.tiles, backward_staged=args.staged,
+                      half_gathers=args.half),
         "plain_fp32": dict(len_storage="f32", mode="exact"),
     }
     runs = {}
@@ -517,7 +521,7 @@ def end_to_end(args, W, theta, sino, prm, tg, torch, stream):
         p = tg.Plan(W["P"], W["S"], W["C"], theta, len_storage=args.len_storage,
                     slices_per_pass=args.slices_per_pass, mode="fast",
                     delta_index=True, forward_tiles=args.tiles,
-                    backward_staged=args.staged)
+                    backward_staged=args.staged, half_gathers=args.half)
         p.set_stream(stream)
         p.set_sinogram(host, apply_abs=True)
         p.reset_recon("pml")
@@ -549,6 +553,9 @@ def main():
                     help="ray-ordered forward projection instead of the tile-staged one")
     ap.add_argument("--staged", action="store_true",
                     help="shared-memory-staged backprojection")
+    ap.add_argument("--no-half-gathers", dest="half", action="store_false",
+                    help="FP32 gather operands instead of halves (shared-memory "
+                         "tile, ratio factors)")
     ap.add_argument("--autotune", action="store_true",
                     help="time the plan configurations on a 16-slice sample first "
                          "and run the fastest")

@@ -12,6 +12,7 @@
  *   DataRegionBase over the sinogram,
  *     src/common/DISP/core/data_region_base.h:48-51    tg_set_sinogram
  *   trace_utils::Absolute, src/common/trace_utils.cc:4-8  tg_set_sinogram(abs=1)
+ *   (no counterpart: sinogram floor before MLEM's ratio)  tg_set_sinogram_clip
  *   trace_utils::DegreeToRadian, trace_utils.cc:10-24   tg_degree_to_radian
  *   trace_utils::Calculate* tracer chain,
  *     src/common/trace_utils.cc:41-216                  tg_trace_rays (export)
@@ -101,6 +102,12 @@ typedef struct {
   int backward_staged;    /* fast mode only: the backprojection stages each
                              16x16-pixel block's detector windows in shared
                              memory instead of gathering through L1 */
+  int half_gathers;       /* fast mode with forward_tiles, L1 backprojection:
+                             tg_iterate keeps the gathered operands as IEEE
+                             halves with FP32 arithmetic - the forward
+                             projection's shared-memory reconstruction tile,
+                             and (MLEM/PML/APMLR) the per-ray factors as
+                             factor - 1 - halving the bytes of both gathers */
 } tg_plan_desc;
 
 typedef struct {
@@ -163,6 +170,14 @@ int tg_degree_to_radian(float* theta, int n);
  * during the upload. */
 int tg_set_sinogram(tg_plan* plan, const float* sino, int on_device,
                     int apply_abs);
+
+/* tg_set_sinogram, then every value below clip_min (after |x| when
+ * apply_abs) is raised to clip_min; NaN stays NaN. No counterpart in the
+ * reference, whose MLEM driver divides by whatever the sinogram holds
+ * (mlem.cc:50-52): a floor such as 1e-6 keeps the ratio step's factors
+ * positive for noisy, log-converted data with zero-count rays. */
+int tg_set_sinogram_clip(tg_plan* plan, const float* sino, int on_device,
+                         int apply_abs, float clip_min);
 
 /* Reconstruction in the reference layout: (S + 2*halo) x C x C float32 where
  * halo = 1 for APMLR (TraceMetadata with num_neighbor_recon_slices = 1) and 0

@@ -5,7 +5,7 @@ import pytest
 
 import trace_gb300 as tg
 from oracle import oracle as O
-from tests._util import rel_l2, theta_uniform
+from tests._util import bits, rel_l2, theta_uniform
 
 pytestmark = pytest.mark.gpu
 
@@ -56,4 +56,61 @@ def test_tiled_forward_storage_kinds_against_fp64(storage):
 def test_forward_tiles_needs_fast_mode():
     with pytest.raises(tg.TraceError) as e:
         tg.Plan(8, 1, 16, theta_uniform(8), forward_tiles=True)
+    assert e.value.status == 1
+
+
+@pytest.mark.parametrize("alg", ["sirt", "mlem", "pml", "apmlr"])
+@pytest.mark.parametrize("K,S", [(4, 4), (8, 9)])
+def test_half_gathers_against_fp64(alg, K, S):
+    """16-bit gather operands (shared-memory tile and ratio factors as halves,
+    FP32 arithmetic): error against the FP64 oracle stays at the level of the
+    16-bit lengths. Small grids converge from far away in few iterations, the
+    loosest case for half factors (rel-L2 bound 2e-4 here; the 2048^2 x 1500
+    workload's 30-iteration error is measured by the benchmark)."""
+    C, P, it = 96, 72, 6
+    th = theta_uniform(P)
+    tabs = O.angle_table(th)
+    from trace_gb300.phantom import ellipse_phantoms
+    sino = O.forward(ellipse_phantoms(C, S, seed=5, texture_sigma=0.02), tabs)
+    kw = dict(beta=0.05) if alg in ("pml", "apmlr") else {}
+    ref = O.run(alg, sino, tables=tabs, n_iter=it, precision=O.F64, **kw)["recon"]
+    prm = tg.default_params(alg, beta=0.05)
+    errs = {}
+    for half in (False, True):
+        plan = tg.Plan(P, S, C, th, slices_per_pass=K, mode="fast", len_storage="u16",
+                       delta_index=True, forward_tiles=True, half_gathers=half)
+        plan.set_sinogram(sino, apply_abs=alg != "sirt")
+        plan.reset_recon(alg)
+        plan.iterate(alg, it, prm)
+        errs[half] = rel_l2(plan.get_recon(alg), ref)
+        plan.close()
+    assert errs[False] < 1e-4, errs
+    assert errs[True] < 2e-4, errs
+
+
+def test_half_gathers_keep_operator_path_fp32():
+    """tg_reduce (the reference's RunParallelReduction) runs the ray-ordered
+    forward with FP32 factors on a half_gathers plan: identical replica."""
+    C, P, S = 64, 40, 4
+    th = theta_uniform(P)
+    rng = np.random.default_rng(7)
+    sino = rng.uniform(0.5, 2.0, (P, S, C)).astype(np.float32)
+    prm = tg.default_params("pml", beta=0.1)
+    reps = []
+    for half in (False, True):
+        plan = tg.Plan(P, S, C, th, slices_per_pass=4, mode="fast", len_storage="u16",
+                       delta_index=True, forward_tiles=True, half_gathers=half)
+        plan.set_sinogram(sino, apply_abs=True)
+        plan.reset_recon("pml")
+        plan.reduce("pml", prm)
+        reps.append(plan.get_replica("pml"))
+        plan.close()
+    assert np.array_equal(bits(reps[0]), bits(reps[1]))
+
+
+@pytest.mark.parametrize("kw", [dict(mode="fast"), dict(mode="exact", forward_tiles=True),
+                                dict(mode="fast", forward_tiles=True, backward_staged=True)])
+def test_half_gathers_needs_tiles_and_l1_backprojection(kw):
+    with pytest.raises(tg.TraceError) as e:
+        tg.Plan(8, 1, 16, theta_uniform(8), half_gathers=True, **kw)
     assert e.value.status == 1

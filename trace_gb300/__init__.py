@@ -30,7 +30,8 @@ STATUS = {0: "OK", 1: "E_ARG", 2: "E_CUDA", 3: "E_NOMEM", 4: "E_STATE",
 EXPORTED = [
     "tg_abi_version", "tg_plan_create", "tg_plan_destroy", "tg_plan_get_info",
     "tg_plan_set_stream", "tg_synchronize", "tg_last_error",
-    "tg_degree_to_radian", "tg_set_sinogram", "tg_reset_recon", "tg_set_recon",
+    "tg_degree_to_radian", "tg_set_sinogram", "tg_set_sinogram_clip",
+    "tg_reset_recon", "tg_set_recon",
     "tg_get_recon", "tg_reduce", "tg_get_replica", "tg_calculate_fg",
     "tg_get_fg", "tg_update_recon", "tg_reset_replica", "tg_iterate",
     "tg_forward_project", "tg_trace_rays", "tg_plan_set_timing",
@@ -53,7 +54,7 @@ class PlanDesc(C.Structure):
                 ("len_storage", C.c_int), ("slices_per_pass", C.c_int),
                 ("mode", C.c_int), ("delta_index", C.c_int),
                 ("apmlr_fixed_offset", C.c_int), ("forward_tiles", C.c_int),
-                ("backward_staged", C.c_int)]
+                ("backward_staged", C.c_int), ("half_gathers", C.c_int)]
 
 
 class Params(C.Structure):
@@ -129,7 +130,7 @@ class Plan:
                  len_storage="f32", slices_per_pass=1, mode="exact",
                  delta_index=False, apmlr_fixed_offset=False, slice_id=0,
                  num_total_slices=None, sin_tab=None, cos_tab=None,
-                 forward_tiles=False, backward_staged=False):
+                 forward_tiles=False, backward_staged=False, half_gathers=False):
         self._lib = load_library()
         self.P, self.S, self.C = int(num_projs), int(num_slices), int(num_cols)
         d = PlanDesc(self.P, self.S, self.C, float(center), int(slice_id),
@@ -138,7 +139,8 @@ class Plan:
                      int(slices_per_pass),
                      MODES[mode] if isinstance(mode, str) else int(mode),
                      int(bool(delta_index)), int(bool(apmlr_fixed_offset)),
-                     int(bool(forward_tiles)), int(bool(backward_staged)))
+                     int(bool(forward_tiles)), int(bool(backward_staged)),
+                     int(bool(half_gathers)))
         theta = np.ascontiguousarray(theta, np.float32)
         if theta.size != self.P:
             raise ValueError("theta must have num_projs entries")
@@ -210,14 +212,20 @@ class Plan:
         return 1 if self._alg(alg) == 3 else 0
 
     # -- data
-    def set_sinogram(self, sino, apply_abs=False):
-        if _is_device(sino):
-            self._chk(self._lib.tg_set_sinogram(self._h, _ptr(sino), 1, int(apply_abs)))
-            return
-        sino = np.ascontiguousarray(sino, np.float32)
-        if sino.shape != (self.P, self.S, self.C):
-            raise ValueError(f"sinogram must be [P][S][C] = {(self.P, self.S, self.C)}")
-        self._chk(self._lib.tg_set_sinogram(self._h, _ptr(sino), 0, int(apply_abs)))
+    def set_sinogram(self, sino, apply_abs=False, clip_min=None):
+        """Upload [P][S][C]; apply_abs: |x| (trace_utils::Absolute); clip_min:
+        raise values below it to it (after |x|)."""
+        dev = _is_device(sino)
+        if not dev:
+            sino = np.ascontiguousarray(sino, np.float32)
+            if sino.shape != (self.P, self.S, self.C):
+                raise ValueError(f"sinogram must be [P][S][C] = {(self.P, self.S, self.C)}")
+        if clip_min is None:
+            self._chk(self._lib.tg_set_sinogram(self._h, _ptr(sino), int(dev),
+                                                int(apply_abs)))
+        else:
+            self._chk(self._lib.tg_set_sinogram_clip(self._h, _ptr(sino), int(dev),
+                                                     int(apply_abs), C.c_float(clip_min)))
 
     def reset_recon(self, alg):
         self._chk(self._lib.tg_reset_recon(self._h, self._alg(alg)))

@@ -11,6 +11,10 @@
 // The tile shape keeps the rays a warp touches at one angle within a short
 // detector window, so the factor gathers share L1 sectors.
 //
+// With half factors (fast mode, ratio algorithms) each factor is read as the
+// half (factor - 1) - half the gather bytes - and sum(len * factor) is
+// rebuilt as W + sum(len * (factor - 1)).
+//
 // Epilogue per slice: SIRT recon += num/W (sirt.cc:21-33), MLEM
 // recon *= num/W (mlem.cc:21-34), PML/APMLR the closed-form root with the
 // penalty's F and G (pml.cc:3-23, apmlr.cc:3-26), written to the other
@@ -24,23 +28,24 @@ namespace {
 constexpr int kWarps = 8;
 constexpr int kBlock = kWarps * 32;
 constexpr int kCoefChunk = 512;  // angles of window coefficients per stage
+// Resident blocks per SM the register allocation is sized for (48 registers
+// a thread at 5): at 6 the 8-slice variants spill inside the angle loop.
+constexpr int kMinBlocks = 5;
 
 // Four angles of one lane's backward-matrix entries: 16 bytes for 16-bit
-// codes (two per angle), 32 bytes for floats.
+// codes (two per angle), 32 bytes for floats. The entries of angles
+// 4i..4i+3, tile t, lane l are the 16-byte words (i*ntiles + t)*32 + l
+// (times two for floats): one contiguous 512-byte row per warp.
 template <int LK>
 struct Quad {
-  uint4 w[LK == LK_F32 ? 2 : 1];
+  static constexpr int kWords = LK == LK_F32 ? 2 : 1;
+  uint4 w[kWords];
 };
 
 template <int LK>
-__device__ __forceinline__ void load_quad(const void* dlen, int64_t pair, Quad<LK>& q) {
-  if constexpr (LK == LK_F32) {
-    const uint4* p = reinterpret_cast<const uint4*>(reinterpret_cast<const float2*>(dlen) + pair);
-    q.w[0] = __ldcs(p);
-    q.w[1] = __ldcs(p + 1);
-  } else {
-    q.w[0] = __ldcs(reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(dlen) + pair));
-  }
+__device__ __forceinline__ void load_quad(const uint4* p, Quad<LK>& q) {
+#pragma unroll
+  for (int i = 0; i < Quad<LK>::kWords; ++i) q.w[i] = __ldcs(p + i);
 }
 
 __device__ __forceinline__ uint32_t pick(const uint4& v, int i) {
@@ -73,10 +78,16 @@ __device__ __forceinline__ void quad_pair(const Quad<LK>& q, int j, float inv_sc
   }
 }
 
-template <int K, bool EXACT, bool PEN>
+// FH: the factors are halves (factor - 1), see k_fwd_finish; the missing
+// sum of lengths is the pixel's total length W, added in the epilogue.
+template <int K, bool EXACT, bool PEN, bool FH>
 __device__ __forceinline__ void accumulate(float (&acc)[K], const float (&rf)[K],
                                            float l, const float* ub) {
-  const Vec<K> u = load_vec<K>(ub);
+  Vec<K> u;
+  if constexpr (FH)
+    u = load_hvec<K, false>(reinterpret_cast<const __half*>(ub));
+  else
+    u = load_vec<K>(ub);
 #pragma unroll
   for (int j = 0; j < K; ++j) {
     if (EXACT)
@@ -87,8 +98,8 @@ __device__ __forceinline__ void accumulate(float (&acc)[K], const float (&rf)[K]
   }
 }
 
-template <int K, int LK, bool EXACT, bool PEN>
-__global__ void __launch_bounds__(kBlock, 6)
+template <int K, int LK, bool EXACT, bool PEN, bool FH>
+__global__ void __launch_bounds__(kBlock, kMinBlocks)
     k_backward(IterArgs A, int batch, const float* __restrict__ cur,
                float* __restrict__ next, const float* __restrict__ upd,
                float* __restrict__ rep_num, int epi) {
@@ -119,20 +130,24 @@ __global__ void __launch_bounds__(kBlock, 6)
   // the fixed-point scale of 16-bit codes is applied once, at the end
   constexpr bool kScaled = (LK == LK_U16) && !EXACT;
   const int P4 = A.M.P4;
-  const int64_t qstride = (int64_t)A.M.ntiles * 32 * 4;  // pairs per 4 angles
+  // walking pointers: this lane's matrix words and the factor rows of the
+  // current four angles
+  constexpr int QW = Quad<LK>::kWords;
+  const uint32_t qstep = (uint32_t)A.M.ntiles * 32 * QW;  // words per 4 angles
+  const uint4* qp = reinterpret_cast<const uint4*>(A.M.dlen) + ((int64_t)tile * 32 + lane) * QW;
+  const int ck = G.C * K;  // factor floats per angle
+  const float* ua = upd;
   for (int a0 = 0; a0 < P4; a0 += kCoefChunk) {
     const int na = min(kCoefChunk, P4 - a0);  // a multiple of 4
     __syncthreads();
     for (int i = threadIdx.x; i < na; i += kBlock) s_coef[i] = A.M.wcoef[a0 + i];
     __syncthreads();
     if (!valid) continue;
-    const float* ua = upd + (int64_t)a0 * G.C * K;
-    int64_t pair = dense_pair(A.M.ntiles, a0, tile, lane);
     Quad<LK> q;
-    load_quad<LK>(A.M.dlen, pair, q);
+    load_quad<LK>(qp, q);
     for (int a4 = 0; a4 < na; a4 += 4) {
       Quad<LK> nq;
-      if (a4 + 4 < na) load_quad<LK>(A.M.dlen, pair + qstride, nq);
+      if (a4 + 4 < na) load_quad<LK>(qp + qstep, nq);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         float l0, l1;
@@ -140,33 +155,43 @@ __global__ void __launch_bounds__(kBlock, 6)
         quad_pair<LK, kScaled>(q, j, A.M.inv_scale, l0, l1, h0, h1);
         if (h0 | h1) {
           const int c0 = window_c0(s_coef[a4 + j], xf, yf);
-          const float* ub = ua + ((int64_t)j * G.C + c0) * K;
-          if (h0) accumulate<K, EXACT, PEN>(acc, rf, l0, ub);
-          if (h1) accumulate<K, EXACT, PEN>(acc, rf, l1, ub + K);
+          const int e = j * ck + c0 * K;  // factor element of ray c0
+          const float* ub = FH ? reinterpret_cast<const float*>(
+                                     reinterpret_cast<const __half*>(ua) + e)
+                               : ua + e;
+          const float* ub1 = FH ? reinterpret_cast<const float*>(
+                                      reinterpret_cast<const __half*>(ub) + K)
+                                : ub + K;
+          if (h0) accumulate<K, EXACT, PEN, FH>(acc, rf, l0, ub);
+          if (h1) accumulate<K, EXACT, PEN, FH>(acc, rf, l1, ub1);
         }
       }
       q = nq;
-      pair += qstride;
-      ua += (int64_t)4 * G.C * K;
+      qp += qstep;
+      ua = FH ? reinterpret_cast<const float*>(reinterpret_cast<const __half*>(ua) + 4 * ck)
+              : ua + 4 * ck;
     }
   }
   if (!valid) return;
+  const float Wp = A.M.W[p];
   if constexpr (kScaled) {
 #pragma unroll
     for (int j = 0; j < K; ++j) acc[j] *= A.M.inv_scale;
   }
-  if (PEN && !EXACT) {
+  if constexpr (FH) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) acc[j] += Wp;
+  }
+  if (PEN && !EXACT) {  // the reconstruction factor, applied once per pixel
     const Vec<K> v = load_vec<K>(fsrc);
 #pragma unroll
-    for (int j = 0; j < K; ++j) rf[j] = v.v[j];
+    for (int j = 0; j < K; ++j) acc[j] = -(v.v[j] * acc[j]);
   }
-  const float Wp = A.M.W[p];
 #pragma unroll
   for (int j = 0; j < K; ++j) {
     const int s = batch * K + j;
     if (s >= A.S) break;
-    float num = acc[j];
-    if (PEN && !EXACT) num = -(rf[j] * acc[j]);
+    const float num = acc[j];
     if (epi == EPI_REPLICA) {
       rep_num[(int64_t)s * g2 + p] = num;
       continue;
@@ -198,12 +223,14 @@ void back_launch(const IterArgs& A, int batch, const float* cur, float* next,
                  const float* upd, float* rep_num, int epi, cudaStream_t st) {
   const int blocks = (A.M.ntiles + kWarps - 1) / kWarps;
   const bool pen = A.alg >= 2;
-#define TG_BACK(E, PN) \
-  k_backward<K, LK, E, PN><<<blocks, kBlock, 0, st>>>(A, batch, cur, next, upd, rep_num, epi)
+#define TG_BACK(E, PN, FH) \
+  k_backward<K, LK, E, PN, FH><<<blocks, kBlock, 0, st>>>(A, batch, cur, next, upd, rep_num, epi)
   if (A.exact) {
-    if (pen) TG_BACK(true, true); else TG_BACK(true, false);
+    if (pen) TG_BACK(true, true, false); else TG_BACK(true, false, false);
+  } else if (A.half_factors) {
+    if (pen) TG_BACK(false, true, true); else TG_BACK(false, false, true);
   } else {
-    if (pen) TG_BACK(false, true); else TG_BACK(false, false);
+    if (pen) TG_BACK(false, true, false); else TG_BACK(false, false, false);
   }
 #undef TG_BACK
 }

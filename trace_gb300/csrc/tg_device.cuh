@@ -6,6 +6,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 namespace tg {
 
@@ -222,6 +223,68 @@ __device__ __forceinline__ void store_vec(float* p, const Vec<K>& r) {
     for (int j = 0; j < K; j += 4)
       *reinterpret_cast<float4*>(p + j) =
           make_float4(r.v[j], r.v[j + 1], r.v[j + 2], r.v[j + 3]);
+  }
+}
+
+// ---- k-slice vectors stored as IEEE halves (16-bit gather operands) ------
+__device__ __forceinline__ float2 half2_bits_to_float2(uint32_t w) {
+  __half2 h;
+  memcpy(&h, &w, 4);
+  return __half22float2(h);
+}
+__device__ __forceinline__ uint32_t float2_to_half2_bits(float a, float b) {
+  const __half2 h = __floats2half2_rn(a, b);
+  uint32_t w;
+  memcpy(&w, &h, 4);
+  return w;
+}
+
+// K halves (2K bytes, one aligned load) -> K floats. SHARED: plain load
+// (shared memory), else a read-only global load.
+template <int K, bool SHARED>
+__device__ __forceinline__ Vec<K> load_hvec(const __half* p) {
+  Vec<K> r;
+  if constexpr (K == 1) {
+    r.v[0] = __half2float(SHARED ? *p : __ldg(p));
+  } else if constexpr (K == 2) {
+    const uint32_t w = SHARED ? *reinterpret_cast<const uint32_t*>(p)
+                              : __ldg(reinterpret_cast<const unsigned int*>(p));
+    const float2 f = half2_bits_to_float2(w);
+    r.v[0] = f.x;
+    r.v[1] = f.y;
+  } else if constexpr (K == 4) {
+    const uint2 w = SHARED ? *reinterpret_cast<const uint2*>(p)
+                           : __ldg(reinterpret_cast<const uint2*>(p));
+    const float2 a = half2_bits_to_float2(w.x), b = half2_bits_to_float2(w.y);
+    r.v[0] = a.x; r.v[1] = a.y; r.v[2] = b.x; r.v[3] = b.y;
+  } else {
+    const uint4 w = SHARED ? *reinterpret_cast<const uint4*>(p)
+                           : __ldg(reinterpret_cast<const uint4*>(p));
+    const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float2 f = half2_bits_to_float2(ws[i]);
+      r.v[2 * i] = f.x;
+      r.v[2 * i + 1] = f.y;
+    }
+  }
+  return r;
+}
+
+// K floats -> K halves (round to nearest), one aligned store.
+template <int K>
+__device__ __forceinline__ void store_hvec(__half* p, const Vec<K>& r) {
+  if constexpr (K == 1) {
+    *p = __float2half_rn(r.v[0]);
+  } else if constexpr (K == 2) {
+    *reinterpret_cast<uint32_t*>(p) = float2_to_half2_bits(r.v[0], r.v[1]);
+  } else if constexpr (K == 4) {
+    *reinterpret_cast<uint2*>(p) = make_uint2(float2_to_half2_bits(r.v[0], r.v[1]),
+                                              float2_to_half2_bits(r.v[2], r.v[3]));
+  } else {
+    *reinterpret_cast<uint4*>(p) = make_uint4(
+        float2_to_half2_bits(r.v[0], r.v[1]), float2_to_half2_bits(r.v[2], r.v[3]),
+        float2_to_half2_bits(r.v[4], r.v[5]), float2_to_half2_bits(r.v[6], r.v[7]));
   }
 }
 

@@ -58,7 +58,8 @@ __global__ void k_update(IterArgs A, float* __restrict__ recon,
 // ---- layouts -----------------------------------------------------------------
 // [P][S][C] -> [ceil(S/K)][P*C][K]
 __global__ void k_sino_pack(const float* __restrict__ in, float* __restrict__ out,
-                            int P, int S, int C, int K, int apply_abs) {
+                            int P, int S, int C, int K, int apply_abs, int clip,
+                            float clip_min) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t n = (int64_t)P * S * C;
   if (i >= n) return;
@@ -68,6 +69,7 @@ __global__ void k_sino_pack(const float* __restrict__ in, float* __restrict__ ou
   const int64_t R = (int64_t)P * C;
   float v = in[i];
   if (apply_abs) v = fabsf(v);
+  if (clip && v < clip_min) v = clip_min;  // NaN fails the test and stays NaN
   out[((int64_t)(s / K) * R + (int64_t)a * C + c) * K + (s % K)] = v;
 }
 
@@ -138,9 +140,10 @@ void launch_update(const IterArgs& A, float* recon, const float* W,
 }
 
 void launch_sino_pack(const float* in, float* out, int P, int S, int C, int K,
-                      int apply_abs, cudaStream_t st) {
+                      int apply_abs, int clip, float clip_min, cudaStream_t st) {
   const int64_t n = (int64_t)P * S * C;
-  k_sino_pack<<<blocks_for(n), kBlock, 0, st>>>(in, out, P, S, C, K, apply_abs);
+  k_sino_pack<<<blocks_for(n), kBlock, 0, st>>>(in, out, P, S, C, K, apply_abs, clip,
+                                                 clip_min);
 }
 
 void launch_sino_unpack(const float* in, float* out, int P, int S, int C,

@@ -70,6 +70,13 @@ struct IterArgs {
   int nslots;
   int slice_id, num_total_slices;  // APMLR top/bottom
   PenaltyWeights pw;
+  // 16-bit gather operands (fast mode, set per launch sequence):
+  // half_tile - the tile-staged forward keeps its shared-memory tile as
+  //             halves; half_factors - the per-ray factors are stored as
+  //             halves of (factor - 1) (ratio algorithms) and the
+  //             backprojection adds the per-pixel total length back
+  int half_tile;
+  int half_factors;
 };
 
 // Address of (slot, pixel) in the batched reconstruction layout.
@@ -130,13 +137,19 @@ void launch_fill64(double* p, int64_t n, double v, cudaStream_t st);
 // tg_tiles.cu
 void launch_runs_count(const DevGeom& G, int tiles_x, int* ray_nruns,
                        cudaStream_t st);
-void launch_runs_emit(const DevGeom& G, int tiles_x, const int64_t* ray_run_off,
+// Run sort key: tile | chunk-count class | ray | ordinal (RunKey).
+struct RunKey {
+  int ray_bits;  // bits of the ray id field
+  __host__ __device__ int class_shift() const { return 8 + ray_bits; }
+  __host__ __device__ int tile_shift() const { return 13 + ray_bits; }
+};
+void launch_runs_emit(const DevGeom& G, int tiles_x, RunKey rk, const int64_t* ray_run_off,
                       unsigned long long* key, int* val, uint16_t* run_lp,
                       uint16_t* run_len, int* tile_count, cudaStream_t st);
 int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
-              int* val_in, int* val_out, int64_t n, int tile_bits,
+              int* val_in, int* val_out, int64_t n, int end_bit,
               cudaStream_t st);
-void launch_runs_group(const unsigned long long* skey, const int* sval,
+void launch_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
                        int64_t nruns, const int* tile_first_run,
                        const int* group_first, const uint16_t* run_lp,
                        const uint16_t* run_len, int* gray, uint16_t* glp,
@@ -157,7 +170,7 @@ void launch_update(const IterArgs& A, float* recon, const float* W,
                    const float* F, const float* Gv, const float* rep_num,
                    cudaStream_t st);
 void launch_sino_pack(const float* in, float* out, int P, int S, int C, int K,
-                      int apply_abs, cudaStream_t st);
+                      int apply_abs, int clip, float clip_min, cudaStream_t st);
 void launch_sino_unpack(const float* in, float* out, int P, int S, int C,
                         int K, cudaStream_t st);
 void launch_recon_pack(const float* in, float* out, int nuser, int g2, int K,

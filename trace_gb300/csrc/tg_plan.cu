@@ -286,7 +286,7 @@ float* batch_ptr(tg_plan* p, float* base, int batch_slot) {
 }
 
 // Tile-ordered forward matrix (tg_tiles.cu): runs of each ray inside 64x64
-// tiles, sorted by (tile, ray) and packed 32 per warp group.
+// tiles, sorted by (tile, chunk-count class, ray) and packed 32 per warp group.
 int build_tiles(tg_plan* p) {
   const DevGeom& G = p->G;
   const int C = p->C;
@@ -294,6 +294,10 @@ int build_tiles(tg_plan* p) {
   const int ntiles = tiles_x * tiles_x;
   int tile_bits = 1;
   while ((1 << tile_bits) < ntiles) ++tile_bits;
+  RunKey rk{1};
+  while ((int64_t(1) << rk.ray_bits) < p->R) ++rk.ray_bits;
+  const int end_bit = rk.tile_shift() + tile_bits;
+  if (end_bit > 64) return fail(p, TG_E_GEOMETRY, "tile run keys exceed 64 bits");
   // temporaries of the construction, freed at the end
   std::vector<std::pair<void*, size_t>> tmp;
   auto talloc = [&](auto** ptr, size_t n, bool zero) -> int {
@@ -330,8 +334,8 @@ int build_tiles(tg_plan* p) {
       (rc = talloc(&tile_count, (size_t)ntiles, true)))
     return release(), rc;
   cudaMemcpyAsync(d_run_off, run_off.data(), p->R * 8, cudaMemcpyHostToDevice, p->st);
-  launch_runs_emit(G, tiles_x, d_run_off, key, val, run_lp, run_len, tile_count, p->st);
-  if (sort_runs(key, key2, val, val2, NR, tile_bits, p->st))
+  launch_runs_emit(G, tiles_x, rk, d_run_off, key, val, run_lp, run_len, tile_count, p->st);
+  if (sort_runs(key, key2, val, val2, NR, end_bit, p->st))
     return release(), fail(p, TG_E_CUDA, "sorting the tile runs failed");
   std::vector<int> tcount(ntiles);
   cudaMemcpyAsync(tcount.data(), tile_count, ntiles * 4, cudaMemcpyDeviceToHost, p->st);
@@ -358,7 +362,7 @@ int build_tiles(tg_plan* p) {
   cudaMemsetAsync(gray, 0xff, (size_t)groups * 32 * 4, p->st);  // empty lanes: -1
   cudaMemcpyAsync(d_tile_first, tile_first.data(), (ntiles + 1) * 4, cudaMemcpyHostToDevice, p->st);
   cudaMemcpyAsync(d_group_first, group_first.data(), (ntiles + 1) * 4, cudaMemcpyHostToDevice, p->st);
-  launch_runs_group(key2, val2, NR, d_tile_first, d_group_first, run_lp, run_len, gray,
+  launch_runs_group(rk, key2, val2, NR, d_tile_first, d_group_first, run_lp, run_len, gray,
                     glp, glen, gsteps, run_slot, p->st);
   std::vector<int> steps(groups);
   cudaMemcpyAsync(steps.data(), gsteps, (size_t)groups * 4, cudaMemcpyDeviceToHost, p->st);
@@ -461,6 +465,9 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     return fail(nullptr, TG_E_ARG, "unknown mode");
   if ((d.forward_tiles || d.backward_staged) && d.mode != TG_MODE_FAST)
     return fail(nullptr, TG_E_ARG, "forward_tiles and backward_staged need fast mode");
+  if (d.half_gathers && (d.mode != TG_MODE_FAST || !d.forward_tiles || d.backward_staged))
+    return fail(nullptr, TG_E_ARG,
+                "half_gathers needs fast mode, forward_tiles and the L1 backprojection");
   if (d.mode == TG_MODE_FP64 &&
       (d.len_storage != TG_LEN_F32 || d.slices_per_pass != 1 || d.delta_index))
     return fail(nullptr, TG_E_ARG,
@@ -762,8 +769,8 @@ int tg_synchronize(tg_plan* p) {
   return TG_OK;
 }
 
-int tg_set_sinogram(tg_plan* p, const float* sino, int on_device,
-                    int apply_abs) {
+static int set_sinogram(tg_plan* p, const float* sino, int on_device,
+                        int apply_abs, int clip, float clip_min) {
   if (!p || !sino) return p ? fail(p, TG_E_ARG, "null sinogram") : TG_E_ARG;
   const size_t n = (size_t)p->P * p->S * p->C;
   if (!p->d_sino) TG_TRY(dalloc(p, &p->d_sino, (size_t)p->nb * p->R * p->K));
@@ -776,10 +783,21 @@ int tg_set_sinogram(tg_plan* p, const float* sino, int on_device,
                                cudaMemcpyHostToDevice, p->st));
     src = p->d_stage;
   }
-  launch_sino_pack(src, p->d_sino, p->P, p->S, p->C, p->K, apply_abs, p->st);
+  launch_sino_pack(src, p->d_sino, p->P, p->S, p->C, p->K, apply_abs, clip, clip_min,
+                   p->st);
   TG_CUDA(p, cudaGetLastError());
   p->have_sino = true;
   return TG_OK;
+}
+
+int tg_set_sinogram(tg_plan* p, const float* sino, int on_device, int apply_abs) {
+  return set_sinogram(p, sino, on_device, apply_abs, 0, 0.f);
+}
+
+int tg_set_sinogram_clip(tg_plan* p, const float* sino, int on_device, int apply_abs,
+                         float clip_min) {
+  if (p && std::isnan(clip_min)) return fail(p, TG_E_ARG, "clip_min is NaN");
+  return set_sinogram(p, sino, on_device, apply_abs, 1, clip_min);
 }
 
 int tg_reset_recon(tg_plan* p, int alg) {
@@ -856,7 +874,12 @@ static int run_forward(tg_plan* p, const IterArgs& A, int b, int out_mode,
 
 // Launches of one fused iteration on the plan's stream (buffers by p->cur;
 // the caller flips p->cur).
-static void issue_iteration(tg_plan* p, const IterArgs& A, int mode) {
+static void issue_iteration(tg_plan* p, const IterArgs& A0, int mode) {
+  IterArgs A = A0;
+  if (p->tiles && p->d.half_gathers) {
+    A.half_tile = 1;
+    A.half_factors = mode == FWD_RATIO;
+  }
   for (int b = 0; b < p->nb; ++b) {
     if (p->tiles) {
       const float* src = batch_ptr(p, p->d_recon[p->cur], b * p->K + p->fshift);

@@ -18,8 +18,8 @@
 // fast mode only.
 //
 // Construction (once per geometry): count runs per ray, emit run records
-// keyed by (tile, ray, ordinal), radix-sort them (CUB), pack each tile's
-// runs into 32-lane groups, then trace again to fill the groups' streams.
+// keyed by (tile, chunk-count class, ray, ordinal), radix-sort them (CUB),
+// pack each tile's runs into 32-lane groups, then trace again to fill the groups' streams.
 #include <cub/device/device_radix_sort.cuh>
 
 #include "tg_kernels.cuh"
@@ -56,8 +56,20 @@ __global__ void __launch_bounds__(kTraceBlock)
   ray_nruns[r] = n;
 }
 
+// A run's sort key: (tile, chunk-count class, ray, ordinal). Within a tile
+// runs of equal 8-step chunk counts (longest first) share warp groups, so
+// the lanes of a group finish together; inside a class the rays stay in
+// order (adjacent rays: shared-memory broadcasts).
+__device__ __forceinline__ unsigned long long run_key(RunKey rk, int t, int len,
+                                                      int64_t r, int k) {
+  const int cls = 31 - min((len + 7) >> 3, 31);
+  return ((unsigned long long)t << rk.tile_shift()) |
+         ((unsigned long long)cls << rk.class_shift()) |
+         ((unsigned long long)r << 8) | (unsigned long long)(k & 255);
+}
+
 __global__ void __launch_bounds__(kTraceBlock)
-    k_runs_emit(DevGeom G, int tiles_x, const int64_t* ray_run_off,
+    k_runs_emit(DevGeom G, int tiles_x, RunKey rk, const int64_t* ray_run_off,
                 unsigned long long* key, int* val, uint16_t* run_lp,
                 uint16_t* run_len, int* tile_count) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -67,7 +79,10 @@ __global__ void __launch_bounds__(kTraceBlock)
   int64_t i = ray_run_off[r] - 1;
   int cur = -1, k = -1, len = 0;
   auto close = [&]() {
-    if (i >= ray_run_off[r]) run_len[i] = (uint16_t)len;
+    if (i >= ray_run_off[r]) {
+      run_len[i] = (uint16_t)len;
+      key[i] = run_key(rk, cur, len, r, k);
+    }
   };
   trace_ray(G, a, c, [&](int idx, float, float) {
     const int ix = idx % g, iy = idx / g;
@@ -78,8 +93,6 @@ __global__ void __launch_bounds__(kTraceBlock)
       ++k;
       cur = t;
       len = 0;
-      key[i] = ((unsigned long long)t << 40) | ((unsigned long long)r << 8) |
-               (unsigned long long)(k & 255);
       val[i] = (int)i;
       run_lp[i] = (uint16_t)((iy % TS) * TS + ix % TS);
       atomicAdd(&tile_count[t], 1);
@@ -89,7 +102,7 @@ __global__ void __launch_bounds__(kTraceBlock)
   close();
 }
 
-__global__ void k_runs_group(const unsigned long long* skey, const int* sval,
+__global__ void k_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
                              int64_t nruns, const int* tile_first_run,
                              const int* group_first, const uint16_t* run_lp,
                              const uint16_t* run_len, int* gray, uint16_t* glp,
@@ -97,13 +110,13 @@ __global__ void k_runs_group(const unsigned long long* skey, const int* sval,
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nruns) return;
   const unsigned long long k = skey[j];
-  const int t = (int)(k >> 40);
+  const int t = (int)(k >> rk.tile_shift());
   const int rank = (int)(j - tile_first_run[t]);
   const int grp = group_first[t] + rank / 32;
   const int lane = rank % 32;
   const int i = sval[j];
   const int slot = grp * 32 + lane;
-  gray[slot] = (int)((k >> 8) & 0xffffffffull);
+  gray[slot] = (int)((k >> 8) & ((1ull << rk.ray_bits) - 1));
   glp[slot] = run_lp[i];
   glen[slot] = run_len[i];
   run_slot[i] = slot;
@@ -162,13 +175,39 @@ __global__ void __launch_bounds__(kTraceBlock)
 
 // ---- forward -------------------------------------------------------------------
 // Shared-memory image of one tile: K floats per pixel as K/4 float4 planes
-// (K >= 4) or one float/float2 plane, row stride RS pixels.
-template <int K>
+// (K >= 4) or one float/float2 plane, row stride RS pixels; with H, K halves
+// per pixel in one plane (one 16-byte read per segment at K = 8).
+template <int K, bool H = false>
 struct TilePlanes {
   static constexpr int kPlanes = K >= 4 ? K / 4 : 1;
   static constexpr int kWidth = K >= 4 ? 4 : K;  // floats per plane entry
-  static constexpr int kBytes = TS * RS * K * 4;
+  static constexpr int kBytes = TS * RS * K * (H ? 2 : 4);
 };
+
+template <int K>
+__device__ __forceinline__ void tile_load_half(__half* sm, const float* __restrict__ recon,
+                                               int g, int x0, int y0) {
+  for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) {
+    const int lx = e % TS, ly = e / TS;
+    const int x = x0 + lx, y = y0 + ly;
+    Vec<K> v;
+    if (x < g && y < g) {
+      v = load_vec<K>(recon + ((int64_t)y * g + x) * K);
+    } else {
+#pragma unroll
+      for (int j = 0; j < K; ++j) v.v[j] = 0.f;
+    }
+    store_hvec<K>(sm + (ly * RS + lx) * K, v);
+  }
+}
+
+template <int K>
+__device__ __forceinline__ void tile_fma_half(const __half* sm, int si, float l,
+                                              float (&acc)[K]) {
+  const Vec<K> v = load_hvec<K, true>(sm + si * K);
+#pragma unroll
+  for (int j = 0; j < K; ++j) acc[j] = fmaf(v.v[j], l, acc[j]);
+}
 
 template <int K>
 __device__ __forceinline__ void tile_load(float* sm, const float* __restrict__ recon,
@@ -277,15 +316,19 @@ __device__ __forceinline__ float chunk_len(const Chunk<LK>& ch, int j,
   }
 }
 
-template <int K, int LK>
+template <int K, int LK, bool H>
 __global__ void __launch_bounds__(kBlock)
     k_forward_tiled(TileMatrixDev T, int g, float inv_scale,
                     const float* __restrict__ recon, float* __restrict__ sim) {
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
+  __half* smh = reinterpret_cast<__half*>(smem4);
   const int t = blockIdx.x;
   const int x0 = (t % T.tiles_x) * TS, y0 = (t / T.tiles_x) * TS;
-  tile_load<K>(sm, recon, g, x0, y0);
+  if constexpr (H)
+    tile_load_half<K>(smh, recon, g, x0, y0);
+  else
+    tile_load<K>(sm, recon, g, x0, y0);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g0 = T.group_first[t], g1 = T.group_first[t + 1];
@@ -314,7 +357,10 @@ __global__ void __launch_bounds__(kBlock)
             lx += (int)(code & 1u);
             ly += (int)(code >> 1) - 1;
           }
-          tile_fma<K>(sm, ly * RS + lx, chunk_len<LK>(cur, j, inv_scale), acc);
+          if constexpr (H)
+            tile_fma_half<K>(smh, ly * RS + lx, chunk_len<LK>(cur, j, inv_scale), acc);
+          else
+            tile_fma<K>(sm, ly * RS + lx, chunk_len<LK>(cur, j, inv_scale), acc);
         }
       }
       cur = nxt;
@@ -323,8 +369,9 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
-// sums -> per-ray factor (as k_forward's epilogue), then clear the sums
-template <int K>
+// sums -> per-ray factor (as k_forward's epilogue), then clear the sums.
+// FH (ratio factors only): the factor is stored as the half (ray/sim - 1).
+template <int K, bool FH>
 __global__ void k_fwd_finish(int64_t nrays, const float* __restrict__ ra2,
                              float* __restrict__ sim, const float* __restrict__ sino,
                              float* __restrict__ out, int out_mode) {
@@ -344,31 +391,46 @@ __global__ void k_fwd_finish(int64_t nrays, const float* __restrict__ ra2,
       o.v[j] = out_mode == FWD_SIRT ? fdiv(fsub(ray.v[j], s.v[j]), a2)
                                     : fdiv(ray.v[j], s.v[j]);
   }
-  store_vec<K>(out + r * K, o);
+  if constexpr (FH) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) o.v[j] -= 1.f;
+    store_hvec<K>(reinterpret_cast<__half*>(out) + r * K, o);
+  } else {
+    store_vec<K>(out + r * K, o);
+  }
   Vec<K> z;
 #pragma unroll
   for (int j = 0; j < K; ++j) z.v[j] = 0.f;
   store_vec<K>(sim + r * K, z);
 }
 
-template <int K, int LK>
+template <int K, int LK, bool H>
 void fwd_tiled_launch(const TileMatrixDev& T, int g, float inv_scale,
                       const float* recon, float* sim, cudaStream_t st) {
-  const int smem = TilePlanes<K>::kBytes;
-  cudaFuncSetAttribute(k_forward_tiled<K, LK>,
+  const int smem = TilePlanes<K, H>::kBytes;
+  cudaFuncSetAttribute(k_forward_tiled<K, LK, H>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  k_forward_tiled<K, LK><<<T.ntiles, kBlock, smem, st>>>(T, g, inv_scale, recon, sim);
+  k_forward_tiled<K, LK, H><<<T.ntiles, kBlock, smem, st>>>(T, g, inv_scale, recon, sim);
 }
 
-template <int K>
+template <int K, bool H>
 void fwd_tiled_kind(const TileMatrixDev& T, int g, int len_kind, float inv_scale,
                     const float* recon, float* sim, cudaStream_t st) {
   switch (len_kind) {
-    case LK_F32: fwd_tiled_launch<K, LK_F32>(T, g, inv_scale, recon, sim, st); break;
-    case LK_BF16: fwd_tiled_launch<K, LK_BF16>(T, g, inv_scale, recon, sim, st); break;
-    case LK_F16: fwd_tiled_launch<K, LK_F16>(T, g, inv_scale, recon, sim, st); break;
-    default: fwd_tiled_launch<K, LK_U16>(T, g, inv_scale, recon, sim, st); break;
+    case LK_F32: fwd_tiled_launch<K, LK_F32, H>(T, g, inv_scale, recon, sim, st); break;
+    case LK_BF16: fwd_tiled_launch<K, LK_BF16, H>(T, g, inv_scale, recon, sim, st); break;
+    case LK_F16: fwd_tiled_launch<K, LK_F16, H>(T, g, inv_scale, recon, sim, st); break;
+    default: fwd_tiled_launch<K, LK_U16, H>(T, g, inv_scale, recon, sim, st); break;
   }
+}
+
+template <int K>
+void fwd_tiled_half(const IterArgs& A, const TileMatrixDev& T, const float* recon,
+                    float* sim, cudaStream_t st) {
+  if (A.half_tile)
+    fwd_tiled_kind<K, true>(T, A.G.C, A.M.len_kind, A.M.inv_scale, recon, sim, st);
+  else
+    fwd_tiled_kind<K, false>(T, A.G.C, A.M.len_kind, A.M.inv_scale, recon, sim, st);
 }
 
 inline int blocks_for(int64_t n, int b) { return (int)((n + b - 1) / b); }
@@ -381,20 +443,19 @@ void launch_runs_count(const DevGeom& G, int tiles_x, int* ray_nruns,
   k_runs_count<<<blocks_for(R, kTraceBlock), kTraceBlock, 0, st>>>(G, tiles_x, ray_nruns);
 }
 
-void launch_runs_emit(const DevGeom& G, int tiles_x, const int64_t* ray_run_off,
+void launch_runs_emit(const DevGeom& G, int tiles_x, RunKey rk, const int64_t* ray_run_off,
                       unsigned long long* key, int* val, uint16_t* run_lp,
                       uint16_t* run_len, int* tile_count, cudaStream_t st) {
   const int64_t R = (int64_t)G.P * G.C;
   k_runs_emit<<<blocks_for(R, kTraceBlock), kTraceBlock, 0, st>>>(
-      G, tiles_x, ray_run_off, key, val, run_lp, run_len, tile_count);
+      G, tiles_x, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
 }
 
 int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
-              int* val_in, int* val_out, int64_t n, int tile_bits,
+              int* val_in, int* val_out, int64_t n, int end_bit,
               cudaStream_t st) {
   size_t bytes = 0;
   if (n > 0x7fffffff) return 3;
-  const int end_bit = 40 + tile_bits;
   cub::DeviceRadixSort::SortPairs(nullptr, bytes, key_in, key_out, val_in, val_out,
                                   (int)n, 0, end_bit, st);
   void* tmp = nullptr;
@@ -406,14 +467,14 @@ int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
   return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
-void launch_runs_group(const unsigned long long* skey, const int* sval,
+void launch_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
                        int64_t nruns, const int* tile_first_run,
                        const int* group_first, const uint16_t* run_lp,
                        const uint16_t* run_len, int* gray, uint16_t* glp,
                        uint16_t* glen, int* gsteps, int* run_slot,
                        cudaStream_t st) {
   k_runs_group<<<blocks_for(nruns, 256), 256, 0, st>>>(
-      skey, sval, nruns, tile_first_run, group_first, run_lp, run_len, gray, glp,
+      rk, skey, sval, nruns, tile_first_run, group_first, run_lp, run_len, gray, glp,
       glen, gsteps, run_slot);
 }
 
@@ -434,24 +495,32 @@ void launch_runs_fill(const DevGeom& G, int tiles_x, int len_kind, float scale,
 
 void launch_forward_tiled(const IterArgs& A, const TileMatrixDev& T,
                           const float* recon_batch, float* sim, cudaStream_t st) {
-  const int g = A.G.C;
   switch (A.K) {
-    case 1: fwd_tiled_kind<1>(T, g, A.M.len_kind, A.M.inv_scale, recon_batch, sim, st); break;
-    case 2: fwd_tiled_kind<2>(T, g, A.M.len_kind, A.M.inv_scale, recon_batch, sim, st); break;
-    case 4: fwd_tiled_kind<4>(T, g, A.M.len_kind, A.M.inv_scale, recon_batch, sim, st); break;
-    default: fwd_tiled_kind<8>(T, g, A.M.len_kind, A.M.inv_scale, recon_batch, sim, st); break;
+    case 1: fwd_tiled_half<1>(A, T, recon_batch, sim, st); break;
+    case 2: fwd_tiled_half<2>(A, T, recon_batch, sim, st); break;
+    case 4: fwd_tiled_half<4>(A, T, recon_batch, sim, st); break;
+    default: fwd_tiled_half<8>(A, T, recon_batch, sim, st); break;
   }
+}
+
+template <int K>
+void fwd_finish_k(const IterArgs& A, float* sim, const float* sino, float* out,
+                  int out_mode, cudaStream_t st) {
+  const int64_t R = (int64_t)A.G.P * A.G.C;
+  const int b = blocks_for(R, 256);
+  if (A.half_factors && out_mode == FWD_RATIO)
+    k_fwd_finish<K, true><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode);
+  else
+    k_fwd_finish<K, false><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode);
 }
 
 void launch_fwd_finish(const IterArgs& A, float* sim, const float* sino,
                        float* out, int out_mode, cudaStream_t st) {
-  const int64_t R = (int64_t)A.G.P * A.G.C;
-  const int b = blocks_for(R, 256);
   switch (A.K) {
-    case 1: k_fwd_finish<1><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode); break;
-    case 2: k_fwd_finish<2><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode); break;
-    case 4: k_fwd_finish<4><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode); break;
-    default: k_fwd_finish<8><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode); break;
+    case 1: fwd_finish_k<1>(A, sim, sino, out, out_mode, st); break;
+    case 2: fwd_finish_k<2>(A, sim, sino, out, out_mode, st); break;
+    case 4: fwd_finish_k<4>(A, sim, sino, out, out_mode, st); break;
+    default: fwd_finish_k<8>(A, sim, sino, out, out_mode, st); break;
   }
 }
 

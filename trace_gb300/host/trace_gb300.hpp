@@ -43,6 +43,9 @@ struct Options {
   int mode = TG_MODE_EXACT;
   int delta_index = 0;
   int apmlr_fixed_offset = 0;
+  int forward_tiles = 0;    // fast mode: tile-staged forward projection
+  int backward_staged = 0;  // fast mode: shared-memory detector windows
+  int half_gathers = 0;     // fast mode + forward_tiles: 16-bit gather operands
 };
 
 // Geometry + reconstruction (TraceMetadata). theta is copied, not owned.
@@ -74,6 +77,9 @@ class GpuTraceMetadata {
     d.mode = opt.mode;
     d.delta_index = opt.delta_index;
     d.apmlr_fixed_offset = opt.apmlr_fixed_offset;
+    d.forward_tiles = opt.forward_tiles;
+    d.backward_staged = opt.backward_staged;
+    d.half_gathers = opt.half_gathers;
     tg_plan* p = nullptr;
     check(tg_plan_create(&d, theta, nullptr, nullptr, &p), nullptr);
     plan_.reset(p);
