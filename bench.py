@@ -334,6 +334,9 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
                  "ms_per_slice_iter": [[c, round(ms, 4)] for c, ms, _ in res]}
         del sample
 
+    # 16-bit gather operands need the tile-staged forward and the L1 backprojection
+    args.half = args.half and args.tiles and not args.staged
+
     # ---- mixed-precision batched path (the measured value)
     plan = tg.Plan(P, S, C, theta, len_storage=args.len_storage, slices_per_pass=K,
                    mode="fast", delta_index=True, forward_tiles=args.tiles,

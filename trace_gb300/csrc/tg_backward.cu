@@ -88,13 +88,13 @@ __device__ __forceinline__ void accumulate(float (&acc)[K], const float (&rf)[K]
     u = load_hvec<K, false>(reinterpret_cast<const __half*>(ub));
   else
     u = load_vec<K>(ub);
+  if constexpr (EXACT) {
 #pragma unroll
-  for (int j = 0; j < K; ++j) {
-    if (EXACT)
+    for (int j = 0; j < K; ++j)
       acc[j] = PEN ? fsub(acc[j], fmul(fmul(rf[j], l), u.v[j]))
                    : fadd(acc[j], fmul(l, u.v[j]));
-    else
-      acc[j] = fmaf(l, u.v[j], acc[j]);
+  } else {
+    fma_slices<K>(acc, l, u.v);
   }
 }
 

@@ -209,13 +209,11 @@ __global__ void __launch_bounds__(kBlock)
             const float* sb = su + (ai * kWin + rel) * Stage<K>::kRay;
             if (h0) {
               const Vec<K> u = lds_vec<K>(sb);
-#pragma unroll
-              for (int k = 0; k < K; ++k) acc[k] = fmaf(l0, u.v[k], acc[k]);
+              fma_slices<K>(acc, l0, u.v);
             }
             if (h1) {
               const Vec<K> u = lds_vec<K>(sb + Stage<K>::kRay);
-#pragma unroll
-              for (int k = 0; k < K; ++k) acc[k] = fmaf(l1, u.v[k], acc[k]);
+              fma_slices<K>(acc, l1, u.v);
             }
           }
         }

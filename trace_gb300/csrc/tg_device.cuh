@@ -161,14 +161,14 @@ template <int LK>
 __device__ __forceinline__ float decode_len(uint16_t v, float inv_scale) {
   if constexpr (LK == LK_BF16) return __bfloat162float(__ushort_as_bfloat16(v));
   else if constexpr (LK == LK_F16) return __half2float(__ushort_as_half(v));
-  else return (float)v * inv_scale;
+  else return u16_to_float(v) * inv_scale;  // exact conversion, no I2F
 }
 
 // 16-bit codes; `kind` is warp-uniform so the switch does not diverge.
 __device__ __forceinline__ float decode16(uint16_t v, int kind, float inv_scale) {
   if (kind == LK_BF16) return __bfloat162float(__ushort_as_bfloat16(v));
   if (kind == LK_F16) return __half2float(__ushort_as_half(v));
-  return (float)v * inv_scale;
+  return u16_to_float(v) * inv_scale;
 }
 __device__ __forceinline__ uint16_t encode16(float x, int kind, float scale) {
   if (kind == LK_BF16) return __bfloat16_as_ushort(__float2bfloat16_rn(x));
@@ -223,6 +223,25 @@ __device__ __forceinline__ void store_vec(float* p, const Vec<K>& r) {
     for (int j = 0; j < K; j += 4)
       *reinterpret_cast<float4*>(p + j) =
           make_float4(r.v[j], r.v[j + 1], r.v[j + 2], r.v[j + 3]);
+  }
+}
+
+// acc[j] += l * v[j] for the K slices, two slices per instruction (the
+// paired single-precision FMA of sm_100 and later); every component is
+// rounded exactly as fmaf rounds it.
+template <int K>
+__device__ __forceinline__ void fma_slices(float (&acc)[K], float l, const float (&v)[K]) {
+  if constexpr (K == 1) {
+    acc[0] = fmaf(v[0], l, acc[0]);
+  } else {
+    const float2 ll = make_float2(l, l);
+#pragma unroll
+    for (int j = 0; j < K; j += 2) {
+      const float2 r = __ffma2_rn(make_float2(v[j], v[j + 1]), ll,
+                                  make_float2(acc[j], acc[j + 1]));
+      acc[j] = r.x;
+      acc[j + 1] = r.y;
+    }
   }
 }
 

@@ -69,9 +69,12 @@ __global__ void __launch_bounds__(kBlock)
       }
       const float l = stream_len<LK>(M.rlen, e, M.inv_scale);
       const Vec<K> v = load_vec<K>(recon + (int64_t)idx * K);
+      if constexpr (EXACT) {
 #pragma unroll
-      for (int j = 0; j < K; ++j)
-        acc[j] = EXACT ? fadd(acc[j], fmul(v.v[j], l)) : fmaf(v.v[j], l, acc[j]);
+        for (int j = 0; j < K; ++j) acc[j] = fadd(acc[j], fmul(v.v[j], l));
+      } else {
+        fma_slices<K>(acc, l, v.v);
+      }
     }
   }
   if (!valid) return;

@@ -205,8 +205,7 @@ template <int K>
 __device__ __forceinline__ void tile_fma_half(const __half* sm, int si, float l,
                                               float (&acc)[K]) {
   const Vec<K> v = load_hvec<K, true>(sm + si * K);
-#pragma unroll
-  for (int j = 0; j < K; ++j) acc[j] = fmaf(v.v[j], l, acc[j]);
+  fma_slices<K>(acc, l, v.v);
 }
 
 template <int K>
@@ -247,10 +246,15 @@ __device__ __forceinline__ void tile_fma(const float* sm, int si, float l,
     const float* src = sm + ((size_t)pl * TS * RS + si) * W;
     if constexpr (W == 4) {
       const float4 v = *reinterpret_cast<const float4*>(src);
-      acc[pl * 4 + 0] = fmaf(v.x, l, acc[pl * 4 + 0]);
-      acc[pl * 4 + 1] = fmaf(v.y, l, acc[pl * 4 + 1]);
-      acc[pl * 4 + 2] = fmaf(v.z, l, acc[pl * 4 + 2]);
-      acc[pl * 4 + 3] = fmaf(v.w, l, acc[pl * 4 + 3]);
+      const float2 ll = make_float2(l, l);
+      const float2 a = __ffma2_rn(make_float2(v.x, v.y), ll,
+                                  make_float2(acc[pl * 4 + 0], acc[pl * 4 + 1]));
+      const float2 b = __ffma2_rn(make_float2(v.z, v.w), ll,
+                                  make_float2(acc[pl * 4 + 2], acc[pl * 4 + 3]));
+      acc[pl * 4 + 0] = a.x;
+      acc[pl * 4 + 1] = a.y;
+      acc[pl * 4 + 2] = b.x;
+      acc[pl * 4 + 3] = b.y;
     } else if constexpr (W == 2) {
       const float2 v = *reinterpret_cast<const float2*>(src);
       acc[0] = fmaf(v.x, l, acc[0]);
@@ -312,7 +316,10 @@ __device__ __forceinline__ float chunk_len(const Chunk<LK>& ch, int j,
   } else {
     const uint4 q = ch.len[0];
     const uint32_t w = (j >> 1) == 0 ? q.x : (j >> 1) == 1 ? q.y : (j >> 1) == 2 ? q.z : q.w;
-    return decode_len<LK>((uint16_t)((j & 1) ? (w >> 16) : (w & 0xffffu)), inv_scale);
+    const uint32_t h = (j & 1) ? (w >> 16) : (w & 0xffffu);
+    // fixed-point codes stay unscaled here; the run's sums are scaled once
+    if constexpr (LK == LK_U16) return u16_to_float(h);
+    else return decode_len<LK>((uint16_t)h, inv_scale);
   }
 }
 
@@ -364,6 +371,10 @@ __global__ void __launch_bounds__(kBlock)
         }
       }
       cur = nxt;
+    }
+    if constexpr (LK == LK_U16) {
+#pragma unroll
+      for (int j = 0; j < K; ++j) acc[j] *= inv_scale;
     }
     if (ray >= 0 && n > 0) red_add<K>(sim + (int64_t)ray * K, acc);
   }
