@@ -26,6 +26,15 @@ Arms
                   the GPU host), all host threads, one slice-iteration of the
                   same geometry per step.
 
+Workloads (--workload): pml2048 (the default above), pml1024 (its small
+case), sirt256 (SIRT 256^2 x 180 angles, 8 slices, 10 iterations, Poisson
+I0=1e4), mlem1024 (MLEM 1024^2 x 720, 64 slices, 20 iterations, I0=5e3,
+sinogram clipped at 1e-6), apmlr2048 (APMLR full volume: 2048 slices of
+2048^2 x 1500 angles, 25 iterations, ellipsoid volume, I0=2e4) and batch64
+(64 independent SIRT/MLEM problems of uneven width, angle count and slice
+count, 15 iterations, advanced together one CUDA-graph launch per iteration
+in waves that fit a device-memory budget).
+
 Multi-GPU: the path is replicated, not sharded (one GPU per plan); under
 torchrun every rank runs the whole workload on its GPU, value = total
 slice-iterations / max time over ranks.
@@ -49,15 +58,70 @@ METRIC = ("slice-iter/s at 2048²×1500 angles, mixed+batched vs plain "
 
 WORKLOADS = {
     # the headline workload
-    "pml2048": dict(C=2048, P=1500, S=128, iters=30, beta=0.05, texture=0.02,
+    "pml2048": dict(alg="pml", C=2048, P=1500, S=128, iters=30, beta=0.05, texture=0.02,
                     plain_slices=8, fp64_slices=1, name=(
                         "PML 8-neighbour quadratic penalty beta=0.05, 2048x2048 grid, "
                         "128 slices, 1500 angles x 2048 columns, 30 iterations")),
     # a small case of the same kernels, for profiling captures and quick runs
-    "pml1024": dict(C=1024, P=720, S=8, iters=30, beta=0.05, texture=0.02,
+    "pml1024": dict(alg="pml", C=1024, P=720, S=8, iters=30, beta=0.05, texture=0.02,
                     plain_slices=8, fp64_slices=1, name=(
                         "PML beta=0.05, 1024x1024 grid, 8 slices, 720 angles")),
+    "sirt256": dict(alg="sirt", C=256, P=180, S=8, iters=10, i0=1e4,
+                    plain_slices=8, fp64_slices=8, name=(
+                        "SIRT, 256x256 grid, 8 slices, 180 angles x 256 columns, "
+                        "10 iterations, Poisson noise I0=1e4")),
+    "mlem1024": dict(alg="mlem", C=1024, P=720, S=64, iters=20, i0=5e3, clip=1e-6,
+                     plain_slices=8, fp64_slices=2, name=(
+                         "MLEM, 1024x1024 grid, 64 slices, 720 angles x 1024 columns, "
+                         "20 iterations, Poisson noise I0=5e3, sinogram clipped at 1e-6")),
+    "apmlr2048": dict(alg="apmlr", C=2048, P=1500, S=2048, iters=25, beta=0.02, i0=2e4,
+                      volume=True, plain_slices=8, fp64_slices=4, name=(
+                          "APMLR 8-neighbour regulariser beta0=0.02 (beta1, delta0, "
+                          "delta1, regw 1), full volume 2048 slices x 2048x2048 grid, "
+                          "1500 angles x 2048 columns, 25 iterations, random-ellipsoid "
+                          "volume, Poisson noise I0=2e4")),
+    # uneven batch: many independent problems advanced together (tg_batch)
+    "batch64": dict(
+        kind="batch", alg="sirt+mlem", n=64, widths=(256, 512, 1024, 1536, 2048),
+        angles=(90, 1800), slices=(1, 16), iters=15, seed=2024, name=(
+            "64 independent sinograms in one CUDA-graph launch per iteration: width "
+            "from {256,512,1024,1536,2048}, angles uniform in [90,1800], 1-16 slices, "
+            "50/50 SIRT/MLEM, 15 iterations, grid = width")),
 }
+
+
+def metric_of(W):
+    return METRIC if W is WORKLOADS["pml2048"] else f"slice-iter/s, {W['name']}"
+
+
+def params_of(W, tg):
+    return tg.default_params(W["alg"], beta=W.get("beta"))
+
+
+def prep_host_sino(W, sino):
+    """Host copy of the preprocessing the plan applies on upload."""
+    import numpy as np
+    if W["alg"] != "sirt":
+        sino = np.abs(sino)
+    if W.get("clip") is not None:
+        sino = np.maximum(sino, np.float32(W["clip"]))
+    return np.ascontiguousarray(sino, np.float32)
+
+
+def host_sample_sino(W, threads):
+    """One slice of the workload's data on the host (oracle projector)."""
+    import numpy as np
+    from oracle import oracle as O
+    from trace_gb300.phantom import ellipse_phantoms, poisson_log
+
+    C, P = W["C"], W["P"]
+    theta = (np.arange(P, dtype=np.float64) * np.pi / P).astype(np.float32)
+    tabs = O.angle_table(theta)
+    ph = ellipse_phantoms(C, 1, seed=1234, texture_sigma=W.get("texture", 0.0))
+    sino = O.forward(ph, tabs, threads=threads)
+    if W.get("i0"):
+        sino = poisson_log(sino, W["i0"], seed=4321, g=C)
+    return tabs, prep_host_sino(W, sino)
 
 
 def peaks():
@@ -162,27 +226,24 @@ def barrier(ws):
 
 
 # ---------------------------------------------------------------------------
+def oracle_iteration(W, tabs, sino, threads):
+    from oracle import oracle as O
+    kw = {"beta": W["beta"]} if W["alg"] in ("pml", "apmlr") else {}
+    O.run(W["alg"], sino, tables=tabs, n_iter=1, threads=threads, apply_abs=0, **kw)
+    return O.port().tor_last_loop_seconds()
+
+
 def cpu_baseline(W, steps=1, threads=None):
     """Oracle port of the reference's threaded CPU path: 1 slice-iteration of
     the workload's geometry per step, all host threads."""
-    import numpy as np
-    from oracle import oracle as O
-    from trace_gb300.phantom import ellipse_phantoms
-
-    C, P = W["C"], W["P"]
     threads = threads or os.cpu_count()
-    theta = (np.arange(P, dtype=np.float64) * np.pi / P).astype(np.float32)
-    tabs = O.angle_table(theta)
-    ph = ellipse_phantoms(C, 1, seed=1234, texture_sigma=W["texture"])
-    sino = O.forward(ph, tabs, threads=threads)
-    secs = []
-    for _ in range(steps):
-        O.run("pml", sino, tables=tabs, n_iter=1, beta=W["beta"], threads=threads)
-        secs.append(O.port().tor_last_loop_seconds())
+    tabs, sino = host_sample_sino(W, threads)
+    secs = [oracle_iteration(W, tabs, sino, threads) for _ in range(steps)]
+    C, P = W["C"], W["P"]
     return {"value": 1.0 / statistics.median(secs), "unit": "slice-iter/s",
             "cores": threads, "kind": "port",
-            "sample": f"1 slice x 1 PML iteration at {C}x{C}, {P} angles "
-                      f"({threads} threads, replicas + tree merge as the "
+            "sample": f"1 slice x 1 {W['alg'].upper()} iteration at {C}x{C}, {P} "
+                      f"angles ({threads} threads, replicas + tree merge as the "
                       f"reference engine); median of {steps}",
             "seconds": secs}
 
@@ -191,36 +252,33 @@ def run_reference(args, W):
     ws, rank, _ = dist_setup(0)
     if rank != 0:
         return
-    import numpy as np
-    from oracle import oracle as O
-    from trace_gb300.phantom import ellipse_phantoms
-
-    C, P = W["C"], W["P"]
     threads = os.cpu_count()
-    theta = (np.arange(P, dtype=np.float64) * np.pi / P).astype(np.float32)
-    tabs = O.angle_table(theta)
-    ph = ellipse_phantoms(C, 1, seed=1234, texture_sigma=W["texture"])
-    sino = O.forward(ph, tabs, threads=threads)
-    for _ in range(args.warmup):
-        O.run("pml", sino, tables=tabs, n_iter=1, beta=W["beta"], threads=threads)
-    secs = []
-    for _ in range(args.steps):
-        O.run("pml", sino, tables=tabs, n_iter=1, beta=W["beta"], threads=threads)
-        secs.append(O.port().tor_last_loop_seconds())
+    if W.get("kind") == "batch":
+        # each step: one slice-iteration of a sample of the batch's problems
+        probs = batch_problems_with_theta(W)
+        for _ in range(args.warmup):
+            batch_cpu_baseline(W, probs)
+        runs = [batch_cpu_baseline(W, probs) for _ in range(args.steps)]
+        secs = [r["seconds"] / r["slice_iters"] for r in runs]
+        sample = runs[0]["sample"] if runs else ""
+    else:
+        tabs, sino = host_sample_sino(W, threads)
+        for _ in range(args.warmup):
+            oracle_iteration(W, tabs, sino, threads)
+        secs = [oracle_iteration(W, tabs, sino, threads) for _ in range(args.steps)]
+        sample = (f"1 slice x 1 {W['alg'].upper()} iteration per step at the workload "
+                  "geometry (oracle port of the reference's threaded CPU path)")
     total = sum(secs)
     val = len(secs) / total
     line = {
-        "metric": METRIC, "value": val, "unit": "slice-iter/s", "impl": "reference",
+        "metric": metric_of(W), "value": val, "unit": "slice-iter/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * total / len(secs), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic: seeded random ellipses + gaussian texture",
+        "data": data_desc(W),
         "config": {"workload": W["name"], "sample": "1 slice-iteration per step"},
         "cpu_baseline": {"value": val, "unit": "slice-iter/s", "cores": threads,
-                         "kind": "port",
-                         "sample": "1 slice x 1 PML iteration per step at the "
-                                   "workload geometry (oracle port of the "
-                                   "reference's threaded CPU path)"},
+                         "kind": "port", "sample": sample},
         "e2e": {"value": val, "unit": "slice-iter/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -228,19 +286,48 @@ def run_reference(args, W):
 
 
 # ---------------------------------------------------------------------------
-def make_data(W, device, plan):
-    """Phantom -> forward projection on the device (the plan's projector)."""
-    import torch
-    from trace_gb300.phantom import ellipse_phantoms_torch
+def data_desc(W):
+    d = ("synthetic: seeded random-ellipsoid volume" if W.get("volume")
+         else "synthetic: seeded random ellipses")
+    if W.get("texture"):
+        d += f" + gaussian texture (sigma {W['texture']})"
+    d += ", projected by the plan's projector"
+    if W.get("i0"):
+        d += f", Poisson counts at I0={W['i0']:g} converted with -log"
+    return d
 
-    C, S = W["C"], W["S"]
-    ph = ellipse_phantoms_torch(C, S, seed=1234, device=device,
-                                texture_sigma=W["texture"])
+
+def make_data(W, device, plan):
+    """Phantom -> forward projection on the device (the plan's projector) ->
+    optional Poisson counting noise."""
+    import torch
+    from trace_gb300.phantom import (ellipse_phantoms_torch, ellipsoid_volume_torch,
+                                     poisson_log_torch)
+
+    C, S, P = W["C"], W["S"], W["P"]
+    if W.get("volume"):
+        ph = torch.empty((S, C, C), dtype=torch.float32, device=device)
+        for z0 in range(0, S, 64):
+            n = min(64, S - z0)
+            ph[z0:z0 + n] = ellipsoid_volume_torch(C, S, seed=1234, device=device,
+                                                   first=z0, count=n)
+    else:
+        ph = ellipse_phantoms_torch(C, S, seed=1234, device=device,
+                                    texture_sigma=W.get("texture", 0.0))
     plan.set_recon("sirt", ph)
-    sino = torch.empty((W["P"], S, C), dtype=torch.float32, device=device)
-    plan.forward_project("sirt", out=sino)
     del ph
+    sino = torch.empty((P, S, C), dtype=torch.float32, device=device)
+    plan.forward_project("sirt", out=sino)
+    if W.get("i0"):
+        step = max(1, (1 << 27) // (S * C))
+        for a0 in range(0, P, step):
+            sino[a0:a0 + step] = poisson_log_torch(sino[a0:a0 + step], W["i0"],
+                                                   seed=4321 + a0, g=C)
     return sino
+
+
+def upload(plan, W, sino):
+    plan.set_sinogram(sino, apply_abs=W["alg"] != "sirt", clip_min=W.get("clip"))
 
 
 def time_iterations(plan, alg, prm, n, stream_ptr, torch):
@@ -257,7 +344,7 @@ def time_iterations(plan, alg, prm, n, stream_ptr, torch):
 LEN_BYTES = {"f32": 4, "bf16": 2, "f16": 2, "u16": 2}
 
 
-def kernel_bytes(info, W, K, len_storage, pen=True):
+def kernel_bytes(info, W, K, len_storage):
     """Algorithmic bytes per launch of the forward and backward kernels.
 
     The per-unit figure of the cached-segment-list formulation: every pass
@@ -266,26 +353,31 @@ def kernel_bytes(info, W, K, len_storage, pen=True):
     pass adds the sinogram row read (4 P C) and one reconstruction read
     (4 g^2), the backprojection the reconstruction read and write (8 g^2)
     and, for the penalised algorithms, F and G written and read back plus
-    the neighbour reads (12 g^2). Summed over both kernels this is
-    2 Nseg (4 + L) / K + 4 P C + 12 g^2 + 12 g^2 per slice-iteration.
+    the neighbour reads (12 g^2; APMLR's two axial neighbours 8 g^2 more).
+    Summed over both kernels this is 2 Nseg (4 + L) / K + 4 P C + 12 g^2
+    (+ 12 g^2 penalised) per slice-iteration.
     """
     C, P = W["C"], W["P"]
     g2 = C * C
+    pen = W["alg"] in ("pml", "apmlr")
     seg = info["num_segments"] * (4 + LEN_BYTES[len_storage])
     fwd = seg + K * (4 * P * C + 4 * g2)
-    back = seg + K * (8 * g2 + (12 * g2 if pen else 0))
+    back = seg + K * (8 * g2 + (12 * g2 if pen else 0)
+                      + (8 * g2 if W["alg"] == "apmlr" else 0))
     return fwd, back
 
 
-def format_bytes(info, W, K, tiles, pen=True):
+def format_bytes(info, W, K, tiles, half=False):
     """Bytes the kernels' own compressed matrix formats move per launch."""
+    pen = W["alg"] in ("pml", "apmlr")
+    fb = 2 if half and W["alg"] != "sirt" else 4  # factor bytes per ray and slice
     C, P = W["C"], W["P"]
     R, g2 = P * C, C * C
     if tiles:  # tile stream + one read of the batch + the ray sums written
         fwd = info["tile_bytes"] + 4 * g2 * K + 4 * R * K
     else:      # matrix + sinogram in, factors out, batch read once
         fwd = info["forward_bytes"] + 4 * R * K * 2 + 4 * g2 * K
-    back = (info["backward_bytes"] + 4 * R * K + 4 * g2 * K * 2 + 4 * g2
+    back = (info["backward_bytes"] + fb * R * K + 4 * g2 * K * 2 + 4 * g2
             + (4 * g2 * K if pen else 0))
     return fwd, back
 
@@ -307,8 +399,9 @@ def run_ours(args, W):
 
 def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     C, P, S = W["C"], W["P"], W["S"]
+    alg = W["alg"]
     theta = (np.arange(P, dtype=np.float64) * np.pi / P).astype(np.float32)
-    prm = tg.default_params("pml", beta=W["beta"])
+    prm = params_of(W, tg)
     K = args.slices_per_pass
     hbm_peak, peak_kind = peaks()
     t0 = time.time()
@@ -321,11 +414,11 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
                      delta_index=True)
         tp.set_stream(stream)
         tp.set_recon("sirt", ellipse_phantoms_torch(C, n, seed=99, device=dev,
-                                                    texture_sigma=W["texture"]))
+                                                    texture_sigma=W.get("texture", 0.0)))
         sample = torch.empty((P, n, C), dtype=torch.float32, device=dev)
         tp.forward_project("sirt", out=sample)
         tp.close()
-        best, res = autotune(theta, sample, "pml", prm, len_storage=args.len_storage,
+        best, res = autotune(theta, sample, alg, prm, len_storage=args.len_storage,
                              stream=stream)
         K, args.tiles, args.staged = (best["slices_per_pass"], best["forward_tiles"],
                                       best["backward_staged"])
@@ -344,16 +437,16 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     plan.set_stream(stream)
     info = plan.info()
     sino = make_data(W, dev, plan)
-    plan.set_sinogram(sino, apply_abs=True)
-    plan.reset_recon("pml")
+    upload(plan, W, sino)
+    plan.reset_recon(alg)
     for _ in range(args.warmup):
-        plan.iterate("pml", 1, prm)
+        plan.iterate(alg, 1, prm)
     torch.cuda.synchronize()
     barrier(ws)
     torch.cuda.synchronize()
     plan.set_timing(True)
     with ClockSampler(local) as clk:
-        ms = time_iterations(plan, "pml", prm, args.steps, stream, torch)
+        ms = time_iterations(plan, alg, prm, args.steps, stream, torch)
     torch.cuda.synchronize()
     barrier(ws)
     tim = plan.timing()
@@ -365,7 +458,7 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     launches = args.steps * nb * (3 if args.tiles else 2)
 
     fwd_b, back_b = kernel_bytes(info, W, K, args.len_storage)
-    fwd_f, back_f = format_bytes(info, W, K, args.tiles)
+    fwd_f, back_f = format_bytes(info, W, K, args.tiles, args.half)
     fwd_avg = tim["forward_ms"] / max(tim["forward_launches"], 1)
     back_avg = tim["backward_ms"] / max(tim["backward_launches"], 1)
     dom = "backward" if tim["backward_ms"] >= tim["forward_ms"] else "forward"
@@ -426,19 +519,18 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     if rank != 0:
         return
     line = {
-        "metric": METRIC, "value": value, "unit": "slice-iter/s",
+        "metric": metric_of(W), "value": value, "unit": "slice-iter/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": f"f32 arithmetic, {args.len_storage} segment lengths",
-        "data": "synthetic: seeded random ellipses + gaussian texture (sigma 0.02), "
-                "projected by the plan's projector",
+        "data": data_desc(W),
         "config": {"workload": W["name"], "slices_per_pass": K,
                    "len_storage": args.len_storage, "index": "4-bit delta",
                    "gather_operands": "f16 (tile, factor-1)" if args.half else "f32",
                    "forward": "tile-staged (64x64 shared-memory tiles)" if args.tiles
                               else "ray-ordered",
-                   "step": f"one PML iteration over all {S} slices",
+                   "step": f"one {alg.upper()} iteration over all {S} slices",
                    "l2": "inputs larger than L2 (system matrix "
                          f"{(info['forward_bytes'] + info['backward_bytes']) / 1e9:.1f} GB "
                          "streamed per step)",
@@ -469,15 +561,16 @@ def fp64_check(args, W, theta, sino, prm, tg, torch, dev):
         "plain_fp32": dict(len_storage="f32", mode="exact"),
     }
     runs = {}
+    alg = W["alg"]
     for key, kw in configs.items():
         p = tg.Plan(W["P"], n, W["C"], theta, **kw)
         p.set_stream(torch.cuda.current_stream().cuda_stream)
-        p.set_sinogram(sub, apply_abs=True)
-        p.reset_recon("pml")
+        upload(p, W, sub)
+        p.reset_recon(alg)
         snaps = []
         for _ in range(W["iters"]):
-            p.iterate("pml", 1, prm)
-            snaps.append(p.get_recon("pml"))
+            p.iterate(alg, 1, prm)
+            snaps.append(p.get_recon(alg))
         runs[key] = snaps
         p.close()
     out = {"slices": n, "iterations": W["iters"], "reference": "GPU FP64 mode"}
@@ -495,13 +588,14 @@ def plain_path(args, W, theta, sino, prm, tg, torch, stream):
                 mode="exact")
     p.set_stream(stream)
     info = p.info()
-    p.set_sinogram(sub, apply_abs=True)
-    p.reset_recon("pml")
+    alg = W["alg"]
+    upload(p, W, sub)
+    p.reset_recon(alg)
     for _ in range(max(1, args.warmup // 2)):
-        p.iterate("pml", 1, prm)
+        p.iterate(alg, 1, prm)
     torch.cuda.synchronize()
     steps = max(2, args.steps // 2)
-    ms = time_iterations(p, "pml", prm, steps, stream, torch)
+    ms = time_iterations(p, alg, prm, steps, stream, torch)
     p.close()
     return {"value": n * steps / (ms / 1000.0), "unit": "slice-iter/s",
             "slices": n, "steps": steps, "setup_ms": info["setup_ms"],
@@ -526,10 +620,10 @@ def end_to_end(args, W, theta, sino, prm, tg, torch, stream):
                     delta_index=True, forward_tiles=args.tiles,
                     backward_staged=args.staged, half_gathers=args.half)
         p.set_stream(stream)
-        p.set_sinogram(host, apply_abs=True)
-        p.reset_recon("pml")
-        p.iterate("pml", W["iters"], prm)
-        p.get_recon("pml", out=None)
+        upload(p, W, host)
+        p.reset_recon(W["alg"])
+        p.iterate(W["alg"], W["iters"], prm)
+        p.get_recon(W["alg"], out=None)
         p.synchronize()
         dt = time.perf_counter() - t
         p.close()
@@ -541,6 +635,187 @@ def end_to_end(args, W, theta, sino, prm, tg, torch, stream):
             "d2h_bytes_per_step": int(out.nbytes),
             "step": f"plan creation + upload + {W['iters']} iterations + download",
             "seconds_per_step": per, "steps": len(times)}
+
+
+def batch_problems(W):
+    import numpy as np
+    rng = np.random.default_rng(W["seed"])
+    n = W["n"]
+    C = rng.choice(W["widths"], n)
+    P = rng.integers(W["angles"][0], W["angles"][1] + 1, n)
+    S = rng.integers(W["slices"][0], W["slices"][1] + 1, n)
+    algs = rng.permutation(["sirt"] * (n // 2) + ["mlem"] * (n - n // 2))
+    return [dict(C=int(c), P=int(p), S=int(s), alg=str(a))
+            for c, p, s, a in zip(C, P, S, algs)]
+
+
+def batch_problems_with_theta(W):
+    import numpy as np
+    probs = batch_problems(W)
+    for pr in probs:
+        pr["theta"] = (np.arange(pr["P"], dtype=np.float64) * np.pi / pr["P"]).astype(np.float32)
+    return probs
+
+
+def batch_plan_kw(pr, args):
+    K = 1
+    while K * 2 <= min(8, pr["S"]):
+        K *= 2
+    return dict(len_storage="u16", slices_per_pass=K, mode="fast", delta_index=True,
+                forward_tiles=True, half_gathers=args.half)
+
+
+def batch_estimate_bytes(pr):
+    """Device bytes of one problem's plan (matrices, tile stream, buffers)."""
+    C, P, S = pr["C"], pr["P"], pr["S"]
+    seg = 1.2 * C * C * P
+    return seg * 5.5 + ((P + 3) // 4 * 4) * C * C * 4 + 16 * C * C * (S + 8) + 12 * P * C * (S + 8)
+
+
+def run_batch(args, W):
+    import numpy as np
+    import torch
+
+    import trace_gb300 as tg
+    from trace_gb300.phantom import ellipse_phantoms_torch
+
+    ws, rank, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ts = torch.cuda.Stream(device=dev)
+    hbm_peak, peak_kind = peaks()
+    t_start = time.time()
+    probs = batch_problems_with_theta(W)
+    with torch.cuda.stream(ts):
+        stream = ts.cuda_stream
+        # inputs: phantom -> projection on the device, kept in pinned host memory
+        hosts = []
+        for i, pr in enumerate(probs):
+            gp = tg.Plan(pr["P"], pr["S"], pr["C"], pr["theta"], mode="fast")
+            gp.set_stream(stream)
+            gp.set_recon("sirt", ellipse_phantoms_torch(pr["C"], pr["S"], seed=1000 + i,
+                                                        device=dev))
+            sino = torch.empty((pr["P"], pr["S"], pr["C"]), dtype=torch.float32, device=dev)
+            gp.forward_project("sirt", out=sino)
+            gp.close()
+            hosts.append(sino.cpu().pin_memory())
+            del sino
+        torch.cuda.synchronize()
+        budget = args.batch_budget_gb * 1e9
+        waves, cur, used = [], [], 0.0
+        for i, pr in enumerate(probs):
+            b = batch_estimate_bytes(pr)
+            if cur and used + b > budget:
+                waves.append(cur)
+                cur, used = [], 0.0
+            cur.append(i)
+            used += b
+        waves.append(cur)
+        iters = W["iters"]
+        e2e_s = iter_ms = setup_ms = alg_bytes = 0.0
+        timed_slice_iters = launches = h2d = d2h = 0
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            for wave in waves:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                plans = []
+                for i in wave:
+                    pr = probs[i]
+                    p = tg.Plan(pr["P"], pr["S"], pr["C"], pr["theta"], **batch_plan_kw(pr, args))
+                    p.set_stream(stream)
+                    p.set_sinogram(hosts[i], apply_abs=pr["alg"] != "sirt")
+                    p.reset_recon(pr["alg"])
+                    plans.append(p)
+                    setup_ms += p.info()["setup_ms"]
+                    h2d += hosts[i].numel() * 4
+                algs = [probs[i]["alg"] for i in wave]
+                batch = tg.Batch(plans)
+                batch.iterate(algs, 1)  # first iteration: captures the graph
+                ev0.record()
+                batch.iterate(algs, iters - 1)
+                ev1.record()
+                outs = [p.get_recon(probs[i]["alg"]) for p, i in zip(plans, wave)]
+                torch.cuda.synchronize()
+                e2e_s += time.perf_counter() - t0
+                iter_ms += ev0.elapsed_time(ev1)
+                for p, i in zip(plans, wave):
+                    pr = probs[i]
+                    info = p.info()
+                    timed_slice_iters += pr["S"] * (iters - 1)
+                    launches += (iters - 1) * info["batches"] * 3
+                    K = batch_plan_kw(pr, args)["slices_per_pass"]
+                    fb, bb = kernel_bytes(info, dict(C=pr["C"], P=pr["P"], alg=pr["alg"]),
+                                          K, "u16")
+                    alg_bytes += (iters - 1) * info["batches"] * (fb + bb)
+                d2h += sum(o.nbytes for o in outs)
+                batch.close()
+                for p in plans:
+                    p.close()
+                del plans, outs
+    ms_max = max_over_ranks(iter_ms, ws)
+    value = timed_slice_iters * ws / (ms_max / 1e3)
+    total_slice_iters = sum(pr["S"] for pr in probs) * W["iters"]
+    achieved = alg_bytes / (iter_ms / 1e3) / 1e9
+    cpu = None
+    if args.cpu_baseline and rank == 0 and ws == 1:
+        cpu = batch_cpu_baseline(W, probs)
+    if rank != 0:
+        return
+    line = {
+        "metric": metric_of(W), "value": value, "unit": "slice-iter/s",
+        "n_gpus": args.gpus, "steps": iters - 1, "warmup": 1,
+        "ms_per_step": iter_ms / (iters - 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 arithmetic, u16 segment lengths"
+                 + (", f16 gather operands" if args.half else ""),
+        "data": "synthetic: seeded random ellipses projected by the plan's projector",
+        "config": {"workload": W["name"], "problems": len(probs),
+                   "waves": len(waves), "wave_budget_gb": args.batch_budget_gb,
+                   "step": "one iteration of every problem of a wave, one CUDA-graph "
+                           "launch (plans forked over up to 16 streams inside the graph)",
+                   "slices_per_pass": "largest power of two <= min(8, slices)",
+                   "l2": "inputs larger than L2 (system matrices streamed per step)",
+                   "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "peak_kind": f"{peak_kind} (burst copy)", "traffic": None,
+                     "kernel": "all kernels of the batch (whole-step effective bandwidth)"},
+        "clocks": clk.summary(), "gpu_launches": launches,
+        "setup_ms": setup_ms,
+        "e2e": {"value": total_slice_iters / e2e_s, "unit": "slice-iter/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "step": "every wave: plan creation (tracing), upload from pinned host, "
+                        f"{iters} iterations, download", "seconds": e2e_s},
+        "cpu_baseline": cpu, "wall_s": time.time() - t_start,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def batch_cpu_baseline(W, probs, sample=4):
+    """The oracle port on a sample of the batch's problems: one slice-iteration
+    of each sampled geometry, all host threads."""
+    import numpy as np
+    from oracle import oracle as O
+    from trace_gb300.phantom import ellipse_phantoms
+    threads = os.cpu_count()
+    rng = np.random.default_rng(W["seed"] + 1)
+    idx = sorted(rng.choice(len(probs), sample, replace=False).tolist())
+    secs = 0.0
+    for i in idx:
+        pr = probs[i]
+        tabs = O.angle_table(pr["theta"])
+        sino = O.forward(ellipse_phantoms(pr["C"], 1, seed=1000 + i), tabs, threads=threads)
+        if pr["alg"] != "sirt":
+            sino = np.abs(sino)
+        O.run(pr["alg"], sino, tables=tabs, n_iter=1, threads=threads)
+        secs += O.port().tor_last_loop_seconds()
+    return {"value": sample / secs, "unit": "slice-iter/s", "cores": threads,
+            "kind": "port", "seconds": secs, "slice_iters": sample,
+            "sample": "1 slice-iteration of each of the problems " + ", ".join(
+                f"{probs[i]['alg']} {probs[i]['C']} columns x {probs[i]['P']} angles"
+                for i in idx)}
 
 
 def main():
@@ -568,12 +843,16 @@ def main():
     ap.add_argument("--no-fp64-check", dest="fp64_check", action="store_false")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--e2e-warmup", type=int, default=1)
+    ap.add_argument("--batch-budget-gb", type=float, default=200.0,
+                    help="batch64: device memory of the plans advanced together")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     W = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, W)
+    elif W.get("kind") == "batch":
+        run_batch(args, W)
     else:
         run_ours(args, W)
 

@@ -154,3 +154,59 @@ def ellipsoid_volume_torch(g: int, num_slices: int, seed: int, device, first: in
                 acc = acc + (t / float(e[3 + i])) ** 2
             out[k] += float(e[10]) * (acc <= 1.0).float()
     return out
+
+
+def ellipsoid_params(n_ellipsoids: int, seed: int):
+    """Per ellipsoid: (cx, cy, cz, a, b, c, q0, q1, q2, q3, intensity).
+
+    The 2-D slice generator extended to 3-D: centres uniform in the ball of
+    radius 0.8, semi-axes uniform in [0.05, 0.4], a uniformly random
+    orientation (unit quaternion), intensity uniform in [0.1, 1]; coordinates
+    normalised to the volume half-extent on every axis.
+    """
+    rng = np.random.default_rng(seed)
+    n = n_ellipsoids
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = 0.8 * rng.uniform(0, 1, n) ** (1.0 / 3.0)
+    ctr = d * r[:, None]
+    ax = rng.uniform(0.05, 0.4, (n, 3))
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    inten = rng.uniform(0.1, 1.0, n)
+    return np.concatenate([ctr, ax, q, inten[:, None]], axis=1)
+
+
+def _rotation(q):
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def ellipsoid_volume_torch(g: int, num_slices: int, seed: int, device, first: int = 0,
+                           count: int | None = None, n_ellipsoids: int = 10):
+    """Slices [first, first + count) of a [num_slices][g][g] random-ellipsoid
+    volume (slice index = z), generated on a device."""
+    import torch
+
+    total = num_slices
+    count = num_slices - first if count is None else count
+    prm = ellipsoid_params(n_ellipsoids, seed)
+    u = (torch.arange(g, device=device, dtype=torch.float32) + 0.5 - g / 2) / (g / 2)
+    Y, X = torch.meshgrid(u, u, indexing="ij")
+    out = torch.zeros((count, g, g), dtype=torch.float32, device=device)
+    for k in range(count):
+        z = (first + k + 0.5 - total / 2) / (total / 2)
+        for e in prm:
+            R = _rotation(e[6:10])  # body axes as columns
+            dz = z - e[2]
+            if abs(dz) > e[3:6].max():
+                continue
+            dx, dy = X - float(e[0]), Y - float(e[1])
+            acc = 0.0
+            for i in range(3):
+                t = dx * float(R[0, i]) + dy * float(R[1, i]) + float(dz * R[2, i])
+                acc = acc + (t / float(e[3 + i])) ** 2
+            out[k] += float(e[10]) * (acc <= 1.0).float()
+    return out
