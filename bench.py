@@ -422,9 +422,10 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
                              stream=stream)
         K, args.tiles, args.staged = (best["slices_per_pass"], best["forward_tiles"],
                                       best["backward_staged"])
+        args.otf = best.get("forward_on_the_fly", False)
         args.slices_per_pass = K
         tuned = {"chosen": best, "sample_slices": n,
-                 "ms_per_slice_iter": [[c, round(ms, 4)] for c, ms, _ in res]}
+                 "ms_per_slice_iter": [[c, round(ms, 4)] for c, ms, _, _ in res]}
         del sample
 
     # 16-bit gather operands need the tile-staged forward and the L1 backprojection
@@ -433,7 +434,8 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     # ---- mixed-precision batched path (the measured value)
     plan = tg.Plan(P, S, C, theta, len_storage=args.len_storage, slices_per_pass=K,
                    mode="fast", delta_index=True, forward_tiles=args.tiles,
-                   backward_staged=args.staged, half_gathers=args.half)
+                   backward_staged=args.staged, half_gathers=args.half,
+                   forward_on_the_fly=args.otf)
     plan.set_stream(stream)
     info = plan.info()
     sino = make_data(W, dev, plan)
@@ -528,6 +530,7 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
         "config": {"workload": W["name"], "slices_per_pass": K,
                    "len_storage": args.len_storage, "index": "4-bit delta",
                    "gather_operands": "f16 (tile, factor-1)" if args.half else "f32",
+                   "intersections": "traced on the fly" if args.otf else "cached",
                    "forward": "tile-staged (64x64 shared-memory tiles)" if args.tiles
                               else "ray-ordered",
                    "step": f"one {alg.upper()} iteration over all {S} slices",
@@ -834,6 +837,9 @@ def main():
     ap.add_argument("--no-half-gathers", dest="half", action="store_false",
                     help="FP32 gather operands instead of halves (shared-memory "
                          "tile, ratio factors)")
+    ap.add_argument("--on-the-fly", dest="otf", action="store_true",
+                    help="no stored ray-ordered forward matrix: rays traced during "
+                         "forward projections")
     ap.add_argument("--autotune", action="store_true",
                     help="time the plan configurations on a 16-slice sample first "
                          "and run the fastest")

@@ -108,6 +108,13 @@ typedef struct {
                              projection's shared-memory reconstruction tile,
                              and (MLEM/PML/APMLR) the per-ray factors as
                              factor - 1 - halving the bytes of both gathers */
+  int forward_on_the_fly; /* not with FP64 mode: no ray-ordered forward matrix
+                             is stored; the forward projections that would
+                             read it (tg_reduce, tg_forward_project, and
+                             tg_iterate without forward_tiles) trace each ray
+                             while projecting it. Saves the matrix's memory
+                             (segments x (L + 4) bytes) for tracing work;
+                             results equal the stored f32 form's */
 } tg_plan_desc;
 
 typedef struct {

@@ -54,7 +54,8 @@ class PlanDesc(C.Structure):
                 ("len_storage", C.c_int), ("slices_per_pass", C.c_int),
                 ("mode", C.c_int), ("delta_index", C.c_int),
                 ("apmlr_fixed_offset", C.c_int), ("forward_tiles", C.c_int),
-                ("backward_staged", C.c_int), ("half_gathers", C.c_int)]
+                ("backward_staged", C.c_int), ("half_gathers", C.c_int),
+                ("forward_on_the_fly", C.c_int)]
 
 
 class Params(C.Structure):
@@ -130,7 +131,8 @@ class Plan:
                  len_storage="f32", slices_per_pass=1, mode="exact",
                  delta_index=False, apmlr_fixed_offset=False, slice_id=0,
                  num_total_slices=None, sin_tab=None, cos_tab=None,
-                 forward_tiles=False, backward_staged=False, half_gathers=False):
+                 forward_tiles=False, backward_staged=False, half_gathers=False,
+                 forward_on_the_fly=False):
         self._lib = load_library()
         self.P, self.S, self.C = int(num_projs), int(num_slices), int(num_cols)
         d = PlanDesc(self.P, self.S, self.C, float(center), int(slice_id),
@@ -140,7 +142,7 @@ class Plan:
                      MODES[mode] if isinstance(mode, str) else int(mode),
                      int(bool(delta_index)), int(bool(apmlr_fixed_offset)),
                      int(bool(forward_tiles)), int(bool(backward_staged)),
-                     int(bool(half_gathers)))
+                     int(bool(half_gathers)), int(bool(forward_on_the_fly)))
         theta = np.ascontiguousarray(theta, np.float32)
         if theta.size != self.P:
             raise ValueError("theta must have num_projs entries")

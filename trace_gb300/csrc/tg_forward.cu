@@ -28,6 +28,31 @@ __device__ __forceinline__ float stream_len(const void* base, int64_t e,
                           inv_scale);
 }
 
+// Per-ray output of the forward kernels: the ray sum (FWD_SIM), SIRT's
+// (ray - sim) / a2 (sirt.cc:50) or the ratio ray / sim (mlem.cc:50,
+// pml.cc:236, apmlr.cc:1017).
+template <int K>
+__device__ __forceinline__ void fwd_epilogue(const MatrixDev& M, int64_t r,
+                                             const float (&acc)[K], const float* sino,
+                                             float* out, int out_mode) {
+  Vec<K> o;
+  if (out_mode == FWD_SIM) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) o.v[j] = acc[j];
+  } else {
+    const Vec<K> ray = load_vec<K>(sino + r * K);
+    if (out_mode == FWD_SIRT) {
+      const float a2 = M.ra2[r];
+#pragma unroll
+      for (int j = 0; j < K; ++j) o.v[j] = fdiv(fsub(ray.v[j], acc[j]), a2);
+    } else {
+#pragma unroll
+      for (int j = 0; j < K; ++j) o.v[j] = fdiv(ray.v[j], acc[j]);
+    }
+  }
+  store_vec<K>(out + r * K, o);
+}
+
 template <int K, int LK, bool EXACT, bool DELTA>
 __global__ void __launch_bounds__(kBlock)
     k_forward(DevGeom G, MatrixDev M, int ngroups,
@@ -78,22 +103,40 @@ __global__ void __launch_bounds__(kBlock)
     }
   }
   if (!valid) return;
-  Vec<K> o;
-  if (out_mode == FWD_SIM) {
+  fwd_epilogue<K>(M, r, acc, sino, out, out_mode);
+}
+
+// On-the-fly forward projection: each ray is traced while it is projected
+// (tg::trace_ray, the reference's tracer) instead of read from a stored
+// matrix. Lengths are the traced float lengths and the sum runs in the
+// reference's segment order, so the exact-mode result equals k_forward's
+// with f32 lengths bit for bit. No forward matrix is kept on the device;
+// the cost moves from streaming the matrix to tracing (ALU).
+template <int K, bool EXACT>
+__global__ void __launch_bounds__(kBlock)
+    k_forward_otf(DevGeom G, MatrixDev M, int ngroups,
+                  const float* __restrict__ recon, const float* __restrict__ sino,
+                  float* __restrict__ out, int out_mode) {
+  const int grp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (grp >= ngroups) return;
+  const int a = grp / G.gpa;
+  const int c = (grp - a * G.gpa) * 32 + lane;
+  if (c >= G.C) return;
+  const int64_t r = (int64_t)a * G.C + c;
+  float acc[K];
 #pragma unroll
-    for (int j = 0; j < K; ++j) o.v[j] = acc[j];
-  } else {
-    const Vec<K> ray = load_vec<K>(sino + r * K);
-    if (out_mode == FWD_SIRT) {
-      const float a2 = M.ra2[r];
+  for (int j = 0; j < K; ++j) acc[j] = 0.f;
+  trace_ray(G, a, c, [&](int idx, float l, float) {
+    const Vec<K> v = load_vec<K>(recon + (int64_t)idx * K);
+    if constexpr (EXACT) {
 #pragma unroll
-      for (int j = 0; j < K; ++j) o.v[j] = fdiv(fsub(ray.v[j], acc[j]), a2);
+      for (int j = 0; j < K; ++j) acc[j] = fadd(acc[j], fmul(v.v[j], l));
     } else {
-#pragma unroll
-      for (int j = 0; j < K; ++j) o.v[j] = fdiv(ray.v[j], acc[j]);
+      fma_slices<K>(acc, l, v.v);
     }
-  }
-  store_vec<K>(out + r * K, o);
+  });
+  fwd_epilogue<K>(M, r, acc, sino, out, out_mode);
 }
 
 template <int K, int LK>
@@ -114,6 +157,17 @@ void fwd_launch(const IterArgs& A, const float* recon, const float* sino,
 template <int K>
 void fwd_kind(const IterArgs& A, const float* recon, const float* sino,
               float* out, int out_mode, cudaStream_t st) {
+  if (A.M.rlen == nullptr) {  // no stored forward matrix: trace on the fly
+    const int ngroups = A.G.P * A.G.gpa;
+    const int blocks = (int)(((int64_t)ngroups * 32 + kBlock - 1) / kBlock);
+    if (A.exact)
+      k_forward_otf<K, true><<<blocks, kBlock, 0, st>>>(A.G, A.M, ngroups, recon, sino,
+                                                         out, out_mode);
+    else
+      k_forward_otf<K, false><<<blocks, kBlock, 0, st>>>(A.G, A.M, ngroups, recon, sino,
+                                                          out, out_mode);
+    return;
+  }
   switch (A.M.len_kind) {
     case LK_F32: fwd_launch<K, LK_F32>(A, recon, sino, out, out_mode, st); break;
     case LK_BF16: fwd_launch<K, LK_BF16>(A, recon, sino, out, out_mode, st); break;

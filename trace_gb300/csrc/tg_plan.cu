@@ -465,6 +465,8 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     return fail(nullptr, TG_E_ARG, "unknown mode");
   if ((d.forward_tiles || d.backward_staged) && d.mode != TG_MODE_FAST)
     return fail(nullptr, TG_E_ARG, "forward_tiles and backward_staged need fast mode");
+  if (d.forward_on_the_fly && d.mode == TG_MODE_FP64)
+    return fail(nullptr, TG_E_ARG, "forward_on_the_fly is not available in FP64 mode");
   if (d.half_gathers && (d.mode != TG_MODE_FAST || !d.forward_tiles || d.backward_staged))
     return fail(nullptr, TG_E_ARG,
                 "half_gathers needs fast mode, forward_tiles and the L1 backprojection");
@@ -596,7 +598,10 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
       (rc = dalloc(p, &p->d_ra2, (size_t)p->R)))
     return bail(rc);
   cudaMemcpyAsync(p->d_roff, roff.data(), ngroups * 8, cudaMemcpyHostToDevice, p->st);
-  if (d.delta_index) {
+  const bool otf = d.forward_on_the_fly != 0;
+  if (otf) {
+    // traced during each forward projection (k_forward_otf)
+  } else if (d.delta_index) {
     if ((rc = dalloc(p, &p->d_rcoff, (size_t)ngroups)) ||
         (rc = dalloc(p, &p->d_rcode, (size_t)words, true)) ||
         (rc = dalloc(p, &p->d_rstart, (size_t)p->R, true)))
@@ -605,7 +610,8 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   } else {
     if ((rc = dalloc(p, &p->d_ridx, (size_t)entries, true))) return bail(rc);
   }
-  if (l16) {
+  if (otf) {
+  } else if (l16) {
     uint16_t* t;
     if ((rc = dalloc(p, &t, (size_t)entries, true))) return bail(rc);
     p->d_rlen = t;
@@ -690,8 +696,9 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
 
   tg_plan_info& I = p->info;
   I.num_segments = nseg_total;
-  I.forward_bytes = entries * (int64_t)lbytes +
-                    (d.delta_index ? words * 4 + p->R * 4 : entries * 4);
+  I.forward_bytes = otf ? 0
+                        : entries * (int64_t)lbytes +
+                              (d.delta_index ? words * 4 + p->R * 4 : entries * 4);
   I.backward_bytes = (int64_t)dense_n * (int64_t)lbytes;
   I.max_segment_length = maxlen;
   I.setup_ms = ms;

@@ -58,10 +58,12 @@ __global__ void __launch_bounds__(kTraceBlock)
   int s = 0, pix = 0, piy = 0;
   uint32_t word = 0;
   unsigned long long bad = 0;
+  const bool store_fwd = rlen != nullptr;  // no forward matrix when traced on the fly
   trace_ray(G, a, c, [&](int idx, float l, float l2) {
     const int64_t e = base + (int64_t)s * 32;
     const int ix = idx % g, iy = idx / g;
-    if (DELTA) {
+    if (!store_fwd) {
+    } else if (DELTA) {
       if (s == 0) {
         rstart[r] = idx;
       } else {
@@ -78,10 +80,12 @@ __global__ void __launch_bounds__(kTraceBlock)
     }
     pix = ix;
     piy = iy;
-    if (L16)
+    if (!store_fwd) {
+    } else if (L16) {
       reinterpret_cast<uint16_t*>(rlen)[e] = encode16(l, M.len_kind, M.scale);
-    else
+    } else {
       reinterpret_cast<float*>(rlen)[e] = l;
+    }
     a2 = fadd(a2, l2);
     a2d = __dadd_rn(a2d, (double)l2);
     // backward matrix: slot = column offset inside the pixel's window
@@ -109,7 +113,7 @@ __global__ void __launch_bounds__(kTraceBlock)
     }
     ++s;
   });
-  if (DELTA && (s & 7) != 0 && s > 0)
+  if (store_fwd && DELTA && (s & 7) != 0 && s > 0)
     rcode[cbase + (int64_t)(s >> 3) * 32] = word;
   ra2[r] = a2;
   if (ra2d) ra2d[r] = a2d;
