@@ -226,23 +226,13 @@ __device__ __forceinline__ void store_vec(float* p, const Vec<K>& r) {
   }
 }
 
-// acc[j] += l * v[j] for the K slices, two slices per instruction (the
-// paired single-precision FMA of sm_100 and later); every component is
-// rounded exactly as fmaf rounds it.
+// acc[j] += l * v[j] for the K slices (fast mode). Scalar FMAs: the paired
+// FP32 FMA of sm_100 (__ffma2_rn) measured slower here - packing the
+// operands into register pairs costs more moves than it saves issue slots.
 template <int K>
 __device__ __forceinline__ void fma_slices(float (&acc)[K], float l, const float (&v)[K]) {
-  if constexpr (K == 1) {
-    acc[0] = fmaf(v[0], l, acc[0]);
-  } else {
-    const float2 ll = make_float2(l, l);
 #pragma unroll
-    for (int j = 0; j < K; j += 2) {
-      const float2 r = __ffma2_rn(make_float2(v[j], v[j + 1]), ll,
-                                  make_float2(acc[j], acc[j + 1]));
-      acc[j] = r.x;
-      acc[j + 1] = r.y;
-    }
-  }
+  for (int j = 0; j < K; ++j) acc[j] = fmaf(v[j], l, acc[j]);
 }
 
 // ---- k-slice vectors stored as IEEE halves (16-bit gather operands) ------

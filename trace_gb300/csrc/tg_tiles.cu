@@ -246,15 +246,10 @@ __device__ __forceinline__ void tile_fma(const float* sm, int si, float l,
     const float* src = sm + ((size_t)pl * TS * RS + si) * W;
     if constexpr (W == 4) {
       const float4 v = *reinterpret_cast<const float4*>(src);
-      const float2 ll = make_float2(l, l);
-      const float2 a = __ffma2_rn(make_float2(v.x, v.y), ll,
-                                  make_float2(acc[pl * 4 + 0], acc[pl * 4 + 1]));
-      const float2 b = __ffma2_rn(make_float2(v.z, v.w), ll,
-                                  make_float2(acc[pl * 4 + 2], acc[pl * 4 + 3]));
-      acc[pl * 4 + 0] = a.x;
-      acc[pl * 4 + 1] = a.y;
-      acc[pl * 4 + 2] = b.x;
-      acc[pl * 4 + 3] = b.y;
+      acc[pl * 4 + 0] = fmaf(v.x, l, acc[pl * 4 + 0]);
+      acc[pl * 4 + 1] = fmaf(v.y, l, acc[pl * 4 + 1]);
+      acc[pl * 4 + 2] = fmaf(v.z, l, acc[pl * 4 + 2]);
+      acc[pl * 4 + 3] = fmaf(v.w, l, acc[pl * 4 + 3]);
     } else if constexpr (W == 2) {
       const float2 v = *reinterpret_cast<const float2*>(src);
       acc[0] = fmaf(v.x, l, acc[0]);
