@@ -468,7 +468,8 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
              "backward": "k_backward"}[dom]
     dom_bytes, dom_ms = (back_b, back_avg) if dom == "backward" else (fwd_b, fwd_avg)
     achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
-    traffic = ncu_traffic().get(f"{kname}:{args.workload}:{args.len_storage}:K{K}")
+    traffic = ncu_traffic().get(f"{kname}:{args.workload}:{args.len_storage}:K{K}"
+                                + (":half" if args.half else ""))
 
     def gbs(b, ms):
         return b / (ms / 1e3) / 1e9 if ms else None
