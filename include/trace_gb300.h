@@ -89,7 +89,8 @@ typedef struct {
   int slice_id;           /* global index of this plan's first slice */
   int num_total_slices;   /* slices in the whole dataset (APMLR top/bottom) */
   int len_storage;        /* tg_len_storage */
-  int slices_per_pass;    /* k in {1,2,4,8}: slices served per matrix read */
+  int slices_per_pass;    /* k in {1,2,4,8,16}: slices served per matrix read
+                             (16 with forward_tiles needs half_gathers) */
   int mode;               /* tg_mode */
   int delta_index;        /* 1 = forward pixel indices delta-coded (4 bits) */
   int apmlr_fixed_offset; /* APMLR only. 0 = reference behaviour: the forward

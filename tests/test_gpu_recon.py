@@ -58,7 +58,7 @@ def test_exact_iterations_match_reference(name, K):
 def test_batching_is_bit_identical_in_exact_mode(name):
     f = golden(name)
     outs = []
-    for K in (1, 2, 4, 8):
+    for K in (1, 2, 4, 8, 16):
         plan = plan_for(f, slices_per_pass=K)
         alg = load(plan, f)
         plan.iterate(alg, int(f["n_iter"]), params_of(f))

@@ -114,3 +114,31 @@ def test_half_gathers_needs_tiles_and_l1_backprojection(kw):
     with pytest.raises(tg.TraceError) as e:
         tg.Plan(8, 1, 16, theta_uniform(8), half_gathers=True, **kw)
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("alg", ["mlem", "pml", "apmlr"])
+def test_sixteen_slices_per_pass_match_eight(alg):
+    C, P, S = 96, 72, 19
+    th = theta_uniform(P)
+    tabs = O.angle_table(th)
+    from trace_gb300.phantom import ellipse_phantoms
+    sino = O.forward(ellipse_phantoms(C, S, seed=17, texture_sigma=0.02), tabs)
+    prm = tg.default_params(alg, beta=0.05)
+    outs = []
+    for K in (8, 16):
+        plan = tg.Plan(P, S, C, th, slices_per_pass=K, mode="fast", len_storage="u16",
+                       delta_index=True, forward_tiles=True, half_gathers=True)
+        plan.set_sinogram(sino, apply_abs=True)
+        plan.reset_recon(alg)
+        plan.iterate(alg, 4, prm)
+        outs.append(plan.get_recon(alg))
+        plan.close()
+    # same arithmetic per slice; the run sums are added in a different order
+    assert rel_l2(outs[1], outs[0]) < 1e-6
+
+
+def test_sixteen_slices_with_tiles_need_half_gathers():
+    with pytest.raises(tg.TraceError) as e:
+        tg.Plan(8, 16, 16, theta_uniform(8), slices_per_pass=16, mode="fast",
+                forward_tiles=True)
+    assert e.value.status == 1

@@ -20,25 +20,27 @@ import time
 from . import Plan, TraceError, default_params
 
 DEFAULT_SPACE = {
-    "slices_per_pass": (4, 8),
+    "slices_per_pass": (4, 8, 16),
     "forward_tiles": (False, True),
     "backward_staged": (False, True),
     "forward_on_the_fly": (False, True),
 }
 
+TG_E_ARG = 1
 TG_E_NOMEM = 3
 
 
 def autotune(theta, sino, alg="pml", params=None, *, len_storage="u16",
              space=None, iters=2, warmup=1, stream=None, log=None,
-             max_device_bytes=None):
+             max_device_bytes=None, fixed=None):
     """Time every configuration of `space` on `sino` ([P][S][C], host array or
     device tensor; S is the sample) and return (best, results).
 
     best: dict of Plan keyword arguments; results: list of
     (config, ms per slice-iteration, plan setup ms, plan device bytes), with
     ms = inf for configurations that did not fit `max_device_bytes` (or the
-    device).
+    device). `fixed`: Plan keyword arguments held for every candidate (e.g.
+    half_gathers); combinations a plan rejects as invalid are skipped.
     """
     space = space or DEFAULT_SPACE
     P, S, C = (int(x) for x in sino.shape)
@@ -53,8 +55,10 @@ def autotune(theta, sino, alg="pml", params=None, *, len_storage="u16",
         t0 = time.perf_counter()
         try:
             plan = Plan(P, S, C, theta, len_storage=len_storage, mode="fast",
-                        delta_index=True, **cfg)
+                        delta_index=True, **{**(fixed or {}), **cfg})
         except TraceError as e:
+            if e.status == TG_E_ARG:
+                continue  # not a valid combination (e.g. half_gathers + staged)
             if e.status != TG_E_NOMEM:
                 raise
             results.append((cfg, math.inf, 0.0, None))

@@ -31,6 +31,7 @@ constexpr int kCoefChunk = 512;  // angles of window coefficients per stage
 // Resident blocks per SM the register allocation is sized for (48 registers
 // a thread at 5): at 6 the 8-slice variants spill inside the angle loop.
 constexpr int kMinBlocks = 5;
+constexpr int kMinBlocks16 = 4;  // 16 slices per pass: 16 accumulators more
 
 // Four angles of one lane's backward-matrix entries: 16 bytes for 16-bit
 // codes (two per angle), 32 bytes for floats. The entries of angles
@@ -99,7 +100,7 @@ __device__ __forceinline__ void accumulate(float (&acc)[K], const float (&rf)[K]
 }
 
 template <int K, int LK, bool EXACT, bool PEN, bool FH>
-__global__ void __launch_bounds__(kBlock, kMinBlocks)
+__global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
     k_backward(IterArgs A, int batch, const float* __restrict__ cur,
                float* __restrict__ next, const float* __restrict__ upd,
                float* __restrict__ rep_num, int epi) {
@@ -255,7 +256,8 @@ void launch_backward(const IterArgs& A, int batch, const float* recon_cur,
     case 1: back_kind<1>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
     case 2: back_kind<2>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
     case 4: back_kind<4>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
-    default: back_kind<8>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
+    case 8: back_kind<8>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
+    default: back_kind<16>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
   }
 }
 

@@ -26,7 +26,7 @@ constexpr int kWin = 24;      // detector columns staged per angle (<= 23 used)
 // bank groups (3 * ray mod 8); K floats otherwise (already conflict-free).
 template <int K>
 struct Stage {
-  static constexpr int kRay = K == 8 ? 12 : K;
+  static constexpr int kRay = K == 8 ? 12 : K == 16 ? 20 : K;
   static constexpr int kUnitBytes = K >= 4 ? 16 : K * 4;
   static constexpr int kUnitsPerRay = K * 4 / kUnitBytes;
   static constexpr int kUnits = kAC * kWin * kUnitsPerRay;  // per chunk
@@ -304,7 +304,8 @@ void launch_backward_staged(const IterArgs& A, int batch, const float* recon_cur
     case 1: staged_kind<1>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
     case 2: staged_kind<2>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
     case 4: staged_kind<4>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
-    default: staged_kind<8>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
+    case 8: staged_kind<8>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
+    default: staged_kind<16>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st); break;
   }
 }
 

@@ -193,12 +193,14 @@ __device__ __forceinline__ Vec<K> load_vec(const float* p) {
     float2 t = __ldg(reinterpret_cast<const float2*>(p));
     r.v[0] = t.x;
     r.v[1] = t.y;
-  } else if constexpr (K == 8) {
-    // one 256-bit read-only load: a single L1 sector lookup per gather
-    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-        : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3]),
-          "=f"(r.v[4]), "=f"(r.v[5]), "=f"(r.v[6]), "=f"(r.v[7])
-        : "l"(p));
+  } else if constexpr (K == 8 || K == 16) {
+    // 256-bit read-only loads: a single L1 sector lookup per 8 slices
+#pragma unroll
+    for (int j = 0; j < K; j += 8)
+      asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+          : "=f"(r.v[j]), "=f"(r.v[j + 1]), "=f"(r.v[j + 2]), "=f"(r.v[j + 3]),
+            "=f"(r.v[j + 4]), "=f"(r.v[j + 5]), "=f"(r.v[j + 6]), "=f"(r.v[j + 7])
+          : "l"(p + j));
   } else {
 #pragma unroll
     for (int j = 0; j < K; j += 4) {
@@ -266,12 +268,31 @@ __device__ __forceinline__ Vec<K> load_hvec(const __half* p) {
                            : __ldg(reinterpret_cast<const uint2*>(p));
     const float2 a = half2_bits_to_float2(w.x), b = half2_bits_to_float2(w.y);
     r.v[0] = a.x; r.v[1] = a.y; r.v[2] = b.x; r.v[3] = b.y;
-  } else {
+  } else if constexpr (K == 8) {
     const uint4 w = SHARED ? *reinterpret_cast<const uint4*>(p)
                            : __ldg(reinterpret_cast<const uint4*>(p));
     const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
+      const float2 f = half2_bits_to_float2(ws[i]);
+      r.v[2 * i] = f.x;
+      r.v[2 * i + 1] = f.y;
+    }
+  } else {  // 16: 32 bytes
+    uint32_t ws[8];
+    if constexpr (SHARED) {
+      const uint4 a = reinterpret_cast<const uint4*>(p)[0];
+      const uint4 b = reinterpret_cast<const uint4*>(p)[1];
+      ws[0] = a.x; ws[1] = a.y; ws[2] = a.z; ws[3] = a.w;
+      ws[4] = b.x; ws[5] = b.y; ws[6] = b.z; ws[7] = b.w;
+    } else {
+      asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+          : "=r"(ws[0]), "=r"(ws[1]), "=r"(ws[2]), "=r"(ws[3]), "=r"(ws[4]),
+            "=r"(ws[5]), "=r"(ws[6]), "=r"(ws[7])
+          : "l"(p));
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
       const float2 f = half2_bits_to_float2(ws[i]);
       r.v[2 * i] = f.x;
       r.v[2 * i + 1] = f.y;
@@ -290,10 +311,12 @@ __device__ __forceinline__ void store_hvec(__half* p, const Vec<K>& r) {
   } else if constexpr (K == 4) {
     *reinterpret_cast<uint2*>(p) = make_uint2(float2_to_half2_bits(r.v[0], r.v[1]),
                                               float2_to_half2_bits(r.v[2], r.v[3]));
-  } else {
-    *reinterpret_cast<uint4*>(p) = make_uint4(
-        float2_to_half2_bits(r.v[0], r.v[1]), float2_to_half2_bits(r.v[2], r.v[3]),
-        float2_to_half2_bits(r.v[4], r.v[5]), float2_to_half2_bits(r.v[6], r.v[7]));
+  } else {  // 8 or 16: one 16-byte store per 8 slices
+#pragma unroll
+    for (int j = 0; j < K; j += 8)
+      *reinterpret_cast<uint4*>(p + j) = make_uint4(
+          float2_to_half2_bits(r.v[j], r.v[j + 1]), float2_to_half2_bits(r.v[j + 2], r.v[j + 3]),
+          float2_to_half2_bits(r.v[j + 4], r.v[j + 5]), float2_to_half2_bits(r.v[j + 6], r.v[j + 7]));
   }
 }
 

@@ -185,7 +185,8 @@ void launch_forward(const IterArgs& A, const float* recon_batch,
     case 1: fwd_kind<1>(A, recon_batch, sino_batch, out, out_mode, st); break;
     case 2: fwd_kind<2>(A, recon_batch, sino_batch, out, out_mode, st); break;
     case 4: fwd_kind<4>(A, recon_batch, sino_batch, out, out_mode, st); break;
-    default: fwd_kind<8>(A, recon_batch, sino_batch, out, out_mode, st); break;
+    case 8: fwd_kind<8>(A, recon_batch, sino_batch, out, out_mode, st); break;
+    default: fwd_kind<16>(A, recon_batch, sino_batch, out, out_mode, st); break;
   }
 }
 

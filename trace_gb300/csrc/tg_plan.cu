@@ -457,8 +457,11 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   if (d.num_cols > 32768)
     return fail(nullptr, TG_E_ARG, "num_cols above 32768 is not supported");
   if (!(d.slices_per_pass == 1 || d.slices_per_pass == 2 ||
-        d.slices_per_pass == 4 || d.slices_per_pass == 8))
-    return fail(nullptr, TG_E_ARG, "slices_per_pass must be 1, 2, 4 or 8");
+        d.slices_per_pass == 4 || d.slices_per_pass == 8 || d.slices_per_pass == 16))
+    return fail(nullptr, TG_E_ARG, "slices_per_pass must be 1, 2, 4, 8 or 16");
+  if (d.slices_per_pass == 16 && d.forward_tiles && !d.half_gathers)
+    return fail(nullptr, TG_E_ARG,
+                "16 slices per pass with forward_tiles needs half_gathers (shared-memory tile)");
   if (d.len_storage < TG_LEN_F32 || d.len_storage > TG_LEN_U16)
     return fail(nullptr, TG_E_ARG, "unknown len_storage");
   if (d.mode != TG_MODE_EXACT && d.mode != TG_MODE_FAST && d.mode != TG_MODE_FP64)

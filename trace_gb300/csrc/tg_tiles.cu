@@ -433,10 +433,15 @@ void fwd_tiled_kind(const TileMatrixDev& T, int g, int len_kind, float inv_scale
 template <int K>
 void fwd_tiled_half(const IterArgs& A, const TileMatrixDev& T, const float* recon,
                     float* sim, cudaStream_t st) {
-  if (A.half_tile)
+  if constexpr (K == 16) {
+    // an f32 tile of 16 slices would not fit shared memory (plan creation
+    // requires half_gathers with 16 slices per pass and forward_tiles)
     fwd_tiled_kind<K, true>(T, A.G.C, A.M.len_kind, A.M.inv_scale, recon, sim, st);
-  else
+  } else if (A.half_tile) {
+    fwd_tiled_kind<K, true>(T, A.G.C, A.M.len_kind, A.M.inv_scale, recon, sim, st);
+  } else {
     fwd_tiled_kind<K, false>(T, A.G.C, A.M.len_kind, A.M.inv_scale, recon, sim, st);
+  }
 }
 
 inline int blocks_for(int64_t n, int b) { return (int)((n + b - 1) / b); }
@@ -505,7 +510,8 @@ void launch_forward_tiled(const IterArgs& A, const TileMatrixDev& T,
     case 1: fwd_tiled_half<1>(A, T, recon_batch, sim, st); break;
     case 2: fwd_tiled_half<2>(A, T, recon_batch, sim, st); break;
     case 4: fwd_tiled_half<4>(A, T, recon_batch, sim, st); break;
-    default: fwd_tiled_half<8>(A, T, recon_batch, sim, st); break;
+    case 8: fwd_tiled_half<8>(A, T, recon_batch, sim, st); break;
+    default: fwd_tiled_half<16>(A, T, recon_batch, sim, st); break;
   }
 }
 
@@ -526,7 +532,8 @@ void launch_fwd_finish(const IterArgs& A, float* sim, const float* sino,
     case 1: fwd_finish_k<1>(A, sim, sino, out, out_mode, st); break;
     case 2: fwd_finish_k<2>(A, sim, sino, out, out_mode, st); break;
     case 4: fwd_finish_k<4>(A, sim, sino, out, out_mode, st); break;
-    default: fwd_finish_k<8>(A, sim, sino, out, out_mode, st); break;
+    case 8: fwd_finish_k<8>(A, sim, sino, out, out_mode, st); break;
+    default: fwd_finish_k<16>(A, sim, sino, out, out_mode, st); break;
   }
 }
 
