@@ -13,7 +13,8 @@
 //
 // With half factors (fast mode, ratio algorithms) each factor is read as the
 // half (factor - 1) - half the gather bytes - and sum(len * factor) is
-// rebuilt as W + sum(len * (factor - 1)).
+// rebuilt as W + sum(len * (factor - 1)), the products taken by
+// mixed-precision FMAs straight from the halves.
 //
 // Epilogue per slice: SIRT recon += num/W (sirt.cc:21-33), MLEM
 // recon *= num/W (mlem.cc:21-34), PML/APMLR the closed-form root with the
@@ -79,11 +80,53 @@ __device__ __forceinline__ void quad_pair(const Quad<LK>& q, int j, float inv_sc
   }
 }
 
+// acc[j] += l * d[j] for K halves d (one aligned load) with the
+// mixed-precision FMA of sm_100 and later (f16 x f16 + f32 -> f32, exact
+// product, one rounding): no half-to-float conversions. The length is
+// rounded to a half; it only multiplies the deviation factor - 1, the bulk
+// sum of lengths (W) is added in FP32 in the epilogue.
+template <int K>
+__device__ __forceinline__ void fma_halves(float (&acc)[K], float l, const __half* p) {
+  const unsigned short lh = __half_as_ushort(__float2half_rn(l));
+  if constexpr (K == 1) {
+    const unsigned short d = __ldg(reinterpret_cast<const unsigned short*>(p));
+    asm("fma.rn.f32.f16 %0, %1, %2, %0;" : "+f"(acc[0]) : "h"(d), "h"(lh));
+  } else {
+    uint32_t ws[K / 2];
+    if constexpr (K == 2) {
+      ws[0] = __ldg(reinterpret_cast<const unsigned int*>(p));
+    } else if constexpr (K == 4) {
+      const uint2 w = __ldg(reinterpret_cast<const uint2*>(p));
+      ws[0] = w.x;
+      ws[1] = w.y;
+    } else {
+#pragma unroll
+      for (int b = 0; b < K / 8; ++b) {
+        const uint4 w = __ldg(reinterpret_cast<const uint4*>(p) + b);
+        ws[4 * b] = w.x;
+        ws[4 * b + 1] = w.y;
+        ws[4 * b + 2] = w.z;
+        ws[4 * b + 3] = w.w;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < K / 2; ++i)
+      asm("{ .reg .b16 lo, hi; mov.b32 {lo, hi}, %2; fma.rn.f32.f16 %0, lo, %3, %0;"
+          " fma.rn.f32.f16 %1, hi, %3, %1; }"
+          : "+f"(acc[2 * i]), "+f"(acc[2 * i + 1])
+          : "r"(ws[i]), "h"(lh));
+  }
+}
+
 // FH: the factors are halves (factor - 1), see k_fwd_finish; the missing
 // sum of lengths is the pixel's total length W, added in the epilogue.
 template <int K, bool EXACT, bool PEN, bool FH>
 __device__ __forceinline__ void accumulate(float (&acc)[K], const float (&rf)[K],
                                            float l, const float* ub) {
+  if constexpr (FH && !EXACT) {
+    fma_halves<K>(acc, l, reinterpret_cast<const __half*>(ub));
+    return;
+  }
   Vec<K> u;
   if constexpr (FH)
     u = load_hvec<K, false>(reinterpret_cast<const __half*>(ub));
@@ -129,7 +172,8 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
 #pragma unroll
   for (int j = 0; j < K; ++j) acc[j] = 0.f;
   // the fixed-point scale of 16-bit codes is applied once, at the end
-  constexpr bool kScaled = (LK == LK_U16) && !EXACT;
+  // (half factors take the scaled length: it is rounded to a half)
+  constexpr bool kScaled = (LK == LK_U16) && !EXACT && !FH;
   const int P4 = A.M.P4;
   // walking pointers: this lane's matrix words and the factor rows of the
   // current four angles
