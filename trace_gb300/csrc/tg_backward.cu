@@ -83,8 +83,9 @@ __device__ __forceinline__ void quad_pair(const Quad<LK>& q, int j, float inv_sc
 // acc[j] += l * d[j] for K halves d (one aligned load) with the
 // mixed-precision FMA of sm_100 and later (f16 x f16 + f32 -> f32, exact
 // product, one rounding): no half-to-float conversions. The length is
-// rounded to a half; it only multiplies the deviation factor - 1, the bulk
-// sum of lengths (W) is added in FP32 in the epilogue.
+// rounded to a half; the epilogue adds, and normalises by, the total of the
+// same half-rounded lengths (Wh), so the backprojection uses one consistent
+// set of lengths: sum(lh * factor) = Wh + sum(lh * (factor - 1)).
 template <int K>
 __device__ __forceinline__ void fma_halves(float (&acc)[K], float l, const __half* p) {
   const unsigned short lh = __half_as_ushort(__float2half_rn(l));
@@ -218,7 +219,8 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
     }
   }
   if (!valid) return;
-  const float Wp = A.M.W[p];
+  // with half factors the lengths are taken as halves: their own total
+  const float Wp = FH ? A.M.Wh[p] : A.M.W[p];
   if constexpr (kScaled) {
 #pragma unroll
     for (int j = 0; j < K; ++j) acc[j] *= A.M.inv_scale;

@@ -30,6 +30,7 @@ struct MatrixDev {
   int tiles_x, ntiles;
   int P4;              // angles rounded up to a multiple of 4 (padding empty)
   const float* W;      // [g*g] total length through each pixel
+  const float* Wh;     // [g*g] the same over half-rounded lengths (half_gathers)
   int len_kind;        // LenKind
   float scale, inv_scale;
 };
@@ -106,7 +107,7 @@ void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
                        double* ra2d, void* dlen, unsigned long long* overflow,
                        cudaStream_t st);
 void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
-                    cudaStream_t st);
+                    cudaStream_t st, bool half_lengths = false);
 void launch_trace_export(const DevGeom& G, const int64_t* offsets, int* idx,
                          float* len, float* len2, cudaStream_t st);
 

@@ -34,6 +34,7 @@ struct tg_plan {
   float* d_ra2 = nullptr;
   void* d_dlen = nullptr;
   float* d_W = nullptr;
+  float* d_Wh = nullptr;  // half_gathers: total of the half-rounded lengths
   // tile-staged forward (fast mode): the tile-ordered matrix + ray sums
   bool tiles = false;
   TileMatrixDev T{};
@@ -634,6 +635,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     p->d_dlen = t;
   }
   if ((rc = dalloc(p, &p->d_W, (size_t)p->g2))) return bail(rc);
+  if (d.half_gathers && (rc = dalloc(p, &p->d_Wh, (size_t)p->g2))) return bail(rc);
   if (p->fp64 && ((rc = dalloc(p, &p->d_ra2d, (size_t)p->R)) ||
                   (rc = dalloc(p, &p->d_W64, (size_t)p->g2))))
     return bail(rc);
@@ -654,6 +656,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   M.ntiles = tiles_x * tiles_y;
   M.P4 = P4;
   M.W = p->d_W;
+  M.Wh = p->d_Wh;
   M.len_kind = p->len_kind;
   M.scale = maxlen > 0 ? 65535.f / maxlen : 1.f;
   M.inv_scale = maxlen > 0 ? maxlen / 65535.f : 1.f;
@@ -662,6 +665,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   launch_trace_fill(G, M, p->d_ridx, p->d_rcode, p->d_rstart, p->d_rlen,
                     p->d_ra2, p->d_ra2d, p->d_dlen, p->d_overflow, p->st);
   launch_weights(G, M, d.mode == TG_MODE_EXACT, p->d_W, p->st);
+  if (p->d_Wh) launch_weights(G, M, 0, p->d_Wh, p->st, true);
   if (p->fp64) launch_weights64(G, M, p->d_W64, p->st);
   unsigned long long overflow = 0;
   cudaMemcpyAsync(&overflow, p->d_overflow, 8, cudaMemcpyDeviceToHost, p->st);

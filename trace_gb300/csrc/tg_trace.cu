@@ -122,7 +122,10 @@ __global__ void __launch_bounds__(kTraceBlock)
 
 // Total length through each pixel: the reference's replica[2p+1]
 // (sirt.cc:59), identical for every slice, so computed once.
-template <bool L16>
+// HALF: the sum of the lengths each rounded to an IEEE half, as the
+// backprojection with half factors multiplies them (its total-length
+// normaliser, so that its lengths are one consistent set).
+template <bool L16, bool HALF>
 __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W) {
   const int g = G.C;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -145,6 +148,10 @@ __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W) {
       const float2 v = reinterpret_cast<const float2*>(M.dlen)[pos >> 1];
       l0 = v.x;
       l1 = v.y;
+    }
+    if constexpr (HALF) {
+      l0 = __half2float(__float2half_rn(l0));
+      l1 = __half2float(__float2half_rn(l1));
     }
     if (exact) {
       sum = fadd(fadd(sum, l0), l1);
@@ -209,12 +216,19 @@ void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
 }
 
 void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
-                    cudaStream_t st) {
+                    cudaStream_t st, bool half_lengths) {
   const int blocks = (int)(((int64_t)M.ntiles * 32 + 255) / 256);
-  if (M.len_kind != LK_F32)
-    k_weights<true><<<blocks, 256, 0, st>>>(G, M, exact, W);
-  else
-    k_weights<false><<<blocks, 256, 0, st>>>(G, M, exact, W);
+  if (M.len_kind != LK_F32) {
+    if (half_lengths)
+      k_weights<true, true><<<blocks, 256, 0, st>>>(G, M, exact, W);
+    else
+      k_weights<true, false><<<blocks, 256, 0, st>>>(G, M, exact, W);
+  } else {
+    if (half_lengths)
+      k_weights<false, true><<<blocks, 256, 0, st>>>(G, M, exact, W);
+    else
+      k_weights<false, false><<<blocks, 256, 0, st>>>(G, M, exact, W);
+  }
 }
 
 void launch_trace_export(const DevGeom& G, const int64_t* offsets, int* idx,
