@@ -381,8 +381,10 @@ int build_tiles(tg_plan* p) {
   uint32_t* tcode;
   void* tlen = nullptr;
   if ((rc = dalloc(p, &d_seg_off, (size_t)groups)) || (rc = dalloc(p, &d_code_off, (size_t)groups)) ||
-      (rc = dalloc(p, &tcode, (size_t)words, true)))
+      (rc = dalloc(p, &tcode, (size_t)words)))
     return release(), rc;
+  // unused steps keep the "stay" code 2 in every nibble (tg_tiles.cu)
+  cudaMemsetAsync(tcode, 0x22, (size_t)words * sizeof(uint32_t), p->st);
   if (l16) {
     uint16_t* t;
     if ((rc = dalloc(p, &t, (size_t)entries, true))) return release(), rc;

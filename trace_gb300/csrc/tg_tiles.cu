@@ -32,6 +32,10 @@ constexpr int TS = kTileSide;     // tile side (pixels)
 constexpr int RS = TS + 1;        // shared-memory row stride (bank spread)
 constexpr int kBlock = 1024;      // forward: 32 warps per tile
 constexpr int kTraceBlock = 128;
+// 4-bit step codes are dx | (dy + 1) << 1; 2 = (0, 0), "stay", never a real
+// step. Every unused nibble of the tile stream holds it (a run's first step,
+// steps past a run's end, empty lanes), with a zero length.
+constexpr uint32_t kStayWord = 0x22222222u;
 
 __device__ __forceinline__ int tile_of(const DevGeom& G, int ix, int iy,
                                        int tiles_x) {
@@ -136,7 +140,7 @@ __global__ void __launch_bounds__(kTraceBlock)
   int64_t i = ray_run_off[r] - 1;
   int cur = -1, s = 0, px = 0, py = 0;
   int64_t lbase = 0, cbase = 0;
-  uint32_t word = 0;
+  uint32_t word = kStayWord;
   auto flush = [&]() {
     if (i >= ray_run_off[r] && (s & 7) != 0) tcode[cbase + (int64_t)(s >> 3) * 32] = word;
   };
@@ -148,13 +152,14 @@ __global__ void __launch_bounds__(kTraceBlock)
       ++i;
       cur = t;
       s = 0;
-      word = 0;
+      word = kStayWord;
       const int slot = run_slot[i];
       const int grp = slot >> 5, lane = slot & 31;
       lbase = gseg_off[grp] + lane * 8;
       cbase = gcode_off[grp] + lane;
     } else {
-      word |= (uint32_t)((ix - px) | ((iy - py + 1) << 1)) << (4 * (s & 7));
+      const int sh = 4 * (s & 7);
+      word = (word & ~(15u << sh)) | ((uint32_t)((ix - px) | ((iy - py + 1) << 1)) << sh);
     }
     // entry (chunk s/8, lane, s%8): chunks of 8 steps, 32 lanes per chunk
     const int64_t e = lbase + (int64_t)(s >> 3) * 256 + (s & 7);
@@ -164,7 +169,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       reinterpret_cast<float*>(tlen)[e] = l;
     if ((s & 7) == 7) {
       tcode[cbase + (int64_t)(s >> 3) * 32] = word;
-      word = 0;
+      word = kStayWord;
     }
     px = ix;
     py = iy;
@@ -339,7 +344,7 @@ __global__ void __launch_bounds__(kBlock)
     const int ray = T.gray[slot];
     const int n = T.glen[slot];
     const int lp = T.glp[slot];
-    int lx = lp % TS, ly = lp / TS;
+    int si = (lp / TS) * RS + lp % TS;  // shared-memory index of the current pixel
     const int chunks = (T.gsteps[grp] + 7) >> 3;
     const int64_t lb = T.gseg_off[grp] + lane * 8;
     const int64_t cb = T.gcode_off[grp] + lane;
@@ -351,19 +356,17 @@ __global__ void __launch_bounds__(kBlock)
     for (int c = 0; c < chunks; ++c) {
       if (c + 1 < chunks) load_chunk<LK>(T, lb, cb, c + 1, nxt);
       const int s0 = c * 8;
+      // No per-step guard: a run's first step and every step past its end
+      // carry the "stay" code and a zero length (see k_runs_fill), so
+      // lanes of shorter runs add 0 * (a finite pixel value) in place.
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        if (s0 + j < n) {
-          if (s0 + j > 0) {
-            const uint32_t code = (cur.code >> (4 * j)) & 15u;
-            lx += (int)(code & 1u);
-            ly += (int)(code >> 1) - 1;
-          }
-          if constexpr (H)
-            tile_fma_half<K>(smh, ly * RS + lx, chunk_len<LK>(cur, j, inv_scale), acc);
-          else
-            tile_fma<K>(sm, ly * RS + lx, chunk_len<LK>(cur, j, inv_scale), acc);
-        }
+        const uint32_t code = (cur.code >> (4 * j)) & 15u;
+        si += (int)(code & 1u) + ((int)(code >> 1) - 1) * RS;
+        if constexpr (H)
+          tile_fma_half<K>(smh, si, chunk_len<LK>(cur, j, inv_scale), acc);
+        else
+          tile_fma<K>(sm, si, chunk_len<LK>(cur, j, inv_scale), acc);
       }
       cur = nxt;
     }
