@@ -571,7 +571,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   if ((rc = dalloc(p, &p->d_rnseg, (size_t)p->R)) ||
       (rc = dalloc(p, &p->d_rcap, (size_t)ngroups)) ||
       (rc = dalloc(p, &p->d_maxlen, 1, true)) ||
-      (rc = dalloc(p, &p->d_overflow, 1, true)))
+      (rc = dalloc(p, &p->d_overflow, 2, true)))
     return bail(rc);
   launch_trace_count(G, p->d_rnseg, p->d_rcap, p->d_maxlen, p->st);
   std::vector<int> rcap(ngroups);
@@ -664,12 +664,15 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   M.inv_scale = maxlen > 0 ? maxlen / 65535.f : 1.f;
 
   // pass 2: fill both matrices; pass 3: total length per pixel
+  cudaMemsetAsync(p->d_overflow + 1, 0xff, sizeof(unsigned long long), p->st);
   launch_trace_fill(G, M, p->d_ridx, p->d_rcode, p->d_rstart, p->d_rlen,
                     p->d_ra2, p->d_ra2d, p->d_dlen, p->d_overflow, p->st);
   launch_weights(G, M, d.mode == TG_MODE_EXACT, p->d_W, p->st);
   if (p->d_Wh) launch_weights(G, M, 0, p->d_Wh, p->st, true);
   if (p->fp64) launch_weights64(G, M, p->d_W64, p->st);
   unsigned long long overflow = 0;
+  unsigned long long first_bad = 0;
+  cudaMemcpyAsync(&first_bad, p->d_overflow + 1, 8, cudaMemcpyDeviceToHost, p->st);
   cudaMemcpyAsync(&overflow, p->d_overflow, 8, cudaMemcpyDeviceToHost, p->st);
   cudaEventRecord(e1, p->st);
   if (cudaStreamSynchronize(p->st) != cudaSuccess) {
@@ -680,7 +683,9 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   if (overflow) {
     p->err = std::to_string(overflow) +
              " segments fall outside the two-column pixel window or the "
-             "4-bit step code; geometry not supported by this layout";
+             "4-bit step code (first: angle " + std::to_string(first_bad >> 32) +
+             ", column " + std::to_string(first_bad & 0xffffffffull) +
+             "); geometry not supported by this layout";
     return bail(TG_E_GEOMETRY);
   }
   if (d.forward_tiles && (rc = build_tiles(p))) {

@@ -117,7 +117,11 @@ __global__ void __launch_bounds__(kTraceBlock)
     rcode[cbase + (int64_t)(s >> 3) * 32] = word;
   ra2[r] = a2;
   if (ra2d) ra2d[r] = a2d;
-  if (bad) atomicAdd(overflow, bad);
+  if (bad) {
+    atomicAdd(overflow, bad);
+    // the first offending ray (lowest angle, then column) for the message
+    atomicMin(overflow + 1, ((unsigned long long)a << 32) | (unsigned)c);
+  }
 }
 
 // Total length through each pixel: the reference's replica[2p+1]
