@@ -136,6 +136,14 @@ typedef struct {
   int batches;                /* ceil(stored slices / slices_per_pass) */
   int64_t tile_bytes;         /* bytes of the tile-ordered forward matrix */
   int64_t tile_runs;          /* runs (ray pieces inside one tile) */
+  int64_t window_exceptions;  /* segments kept apart from the backward matrix:
+                                 the reference's tracer can place a stray
+                                 segment far from its ray (near-vertical
+                                 angles, edge columns); they are added to
+                                 their pixels from a short per-tile list */
+  int forward_traced;         /* 1: the ray-ordered forward projection traces
+                                 its rays on the fly - requested, or a stray
+                                 segment's step did not fit the 4-bit code */
 } tg_plan_info;
 
 typedef struct {

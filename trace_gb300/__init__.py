@@ -68,7 +68,8 @@ class PlanInfo(C.Structure):
                 ("backward_bytes", C.c_int64), ("device_bytes", C.c_int64),
                 ("max_segment_length", C.c_float), ("setup_ms", C.c_double),
                 ("batches", C.c_int), ("tile_bytes", C.c_int64),
-                ("tile_runs", C.c_int64)]
+                ("tile_runs", C.c_int64), ("window_exceptions", C.c_int64),
+                ("forward_traced", C.c_int)]
 
 
 class Timing(C.Structure):

@@ -225,6 +225,14 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
 #pragma unroll
     for (int j = 0; j < K; ++j) acc[j] *= A.M.inv_scale;
   }
+  // segments outside the pixel's window (stored apart, true lengths)
+  for_each_exception(A.M, tile, lane, [&](float l, int ea, int ec) {
+    const int64_t e = ((int64_t)ea * G.C + ec) * K;
+    const float* ub = FH ? reinterpret_cast<const float*>(
+                               reinterpret_cast<const __half*>(upd) + e)
+                         : upd + e;
+    accumulate<K, EXACT, PEN, FH>(acc, rf, l, ub);
+  });
   if constexpr (FH) {
 #pragma unroll
     for (int j = 0; j < K; ++j) acc[j] += Wp;

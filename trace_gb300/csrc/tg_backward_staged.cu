@@ -226,6 +226,11 @@ __global__ void __launch_bounds__(kBlock)
 #pragma unroll
     for (int k = 0; k < K; ++k) acc[k] *= A.M.inv_scale;
   }
+  // segments outside the pixel's window (stored apart, true lengths)
+  for_each_exception(A.M, tile, lane, [&](float l, int ea, int ec) {
+    const Vec<K> u = load_vec<K>(upd + ((int64_t)ea * G.C + ec) * K);
+    fma_slices<K>(acc, l, u.v);
+  });
   float rf[K];
   if (PEN) {
     const Vec<K> v = load_vec<K>(cur + ((int64_t)((batch * K + A.fshift) / K) * g2 + p) * K);

@@ -54,6 +54,8 @@ __global__ void k_weights64(DevGeom G, MatrixDev M, double* W) {
     const float2 v = d[dense_pair(M.ntiles, a, tile, lane)];
     sum = __dadd_rn(__dadd_rn(sum, (double)v.x), (double)v.y);
   }
+  for_each_exception(M, tile, lane,
+                     [&](float l, int, int) { sum = __dadd_rn(sum, (double)l); });
   W[(int64_t)y * g + x] = sum;
 }
 
@@ -89,6 +91,12 @@ __global__ void __launch_bounds__(kBlock)
       acc = pen ? __dsub_rn(acc, __dmul_rn(__dmul_rn(rf, (double)v.y), ub[1]))
                 : __dadd_rn(acc, __dmul_rn((double)v.y, ub[1]));
   }
+  // segments outside the pixel's window (stored apart)
+  for_each_exception(A.M, tile, lane, [&](float l, int ea, int ec) {
+    const double u = upd[(int64_t)ea * G.C + ec];
+    acc = pen ? __dsub_rn(acc, __dmul_rn(__dmul_rn(rf, (double)l), u))
+              : __dadd_rn(acc, __dmul_rn((double)l, u));
+  });
   const int ts = s + A.vshift;
   const int64_t at = (int64_t)ts * g2 + p;
   const double old = cur[at];

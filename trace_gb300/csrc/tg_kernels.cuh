@@ -27,6 +27,12 @@ struct MatrixDev {
   // ray (a, window_c0 + slot) through the pixel
   const void* dlen;
   const float4* wcoef; // [P4] window coefficients {-sin, cos, D, 0}
+  // segments outside their pixel's two-column window (rare: the reference's
+  // tracer puts a stray segment far from its ray at some near-vertical
+  // angles): per 8x4 tile t, entries exc[exc_first[t] .. exc_first[t+1]) =
+  // {lane, angle, column, length bits}; exc_first == nullptr when none
+  const int* exc_first;
+  const int4* exc;
   int tiles_x, ntiles;
   int P4;              // angles rounded up to a multiple of 4 (padding empty)
   const float* W;      // [g*g] total length through each pixel
@@ -105,7 +111,20 @@ void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
 void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
                        uint32_t* rcode, int* rstart, void* rlen, float* ra2,
                        double* ra2d, void* dlen, unsigned long long* overflow,
-                       cudaStream_t st);
+                       int4* exc, int* exc_tile, int exc_cap, cudaStream_t st);
+
+// Adds the window exceptions of the calling lane's pixel: f(l, angle,
+// column) for each, after the regular angle loop.
+template <typename F>
+__device__ __forceinline__ void for_each_exception(const MatrixDev& M, int tile,
+                                                   int lane, F&& f) {
+  if (M.exc_first == nullptr) return;
+  const int e1 = M.exc_first[tile + 1];
+  for (int e = M.exc_first[tile]; e < e1; ++e) {
+    const int4 x = M.exc[e];
+    if (x.x == lane) f(__int_as_float(x.w), x.y, x.z);
+  }
+}
 void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
                     cudaStream_t st, bool half_lengths = false);
 void launch_trace_export(const DevGeom& G, const int64_t* offsets, int* idx,

@@ -1,6 +1,7 @@
 // Host side of the C ABI declared in include/trace_gb300.h: plan creation
 // (geometry tables, tracing, matrix construction), state upload/download,
 // and the per-iteration launch sequence.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -35,6 +36,8 @@ struct tg_plan {
   void* d_dlen = nullptr;
   float* d_W = nullptr;
   float* d_Wh = nullptr;  // half_gathers: total of the half-rounded lengths
+  int* d_exc_first = nullptr;  // window exceptions (CSR over 8x4 tiles)
+  int4* d_exc = nullptr;
   // tile-staged forward (fast mode): the tile-ordered matrix + ray sums
   bool tiles = false;
   TileMatrixDev T{};
@@ -571,7 +574,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   if ((rc = dalloc(p, &p->d_rnseg, (size_t)p->R)) ||
       (rc = dalloc(p, &p->d_rcap, (size_t)ngroups)) ||
       (rc = dalloc(p, &p->d_maxlen, 1, true)) ||
-      (rc = dalloc(p, &p->d_overflow, 2, true)))
+      (rc = dalloc(p, &p->d_overflow, 3, true)))
     return bail(rc);
   launch_trace_count(G, p->d_rnseg, p->d_rcap, p->d_maxlen, p->st);
   std::vector<int> rcap(ngroups);
@@ -664,30 +667,82 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   M.inv_scale = maxlen > 0 ? maxlen / 65535.f : 1.f;
 
   // pass 2: fill both matrices; pass 3: total length per pixel
+  constexpr int kExcCap = 1 << 16;  // window exceptions a plan accepts
+  int4* d_exc_tmp = nullptr;
+  int* d_exc_tile_tmp = nullptr;
+  if ((rc = dalloc(p, &d_exc_tmp, (size_t)kExcCap)) ||
+      (rc = dalloc(p, &d_exc_tile_tmp, (size_t)kExcCap)))
+    return bail(rc);
   cudaMemsetAsync(p->d_overflow + 1, 0xff, sizeof(unsigned long long), p->st);
   launch_trace_fill(G, M, p->d_ridx, p->d_rcode, p->d_rstart, p->d_rlen,
-                    p->d_ra2, p->d_ra2d, p->d_dlen, p->d_overflow, p->st);
-  launch_weights(G, M, d.mode == TG_MODE_EXACT, p->d_W, p->st);
-  if (p->d_Wh) launch_weights(G, M, 0, p->d_Wh, p->st, true);
-  if (p->fp64) launch_weights64(G, M, p->d_W64, p->st);
-  unsigned long long overflow = 0;
-  unsigned long long first_bad = 0;
-  cudaMemcpyAsync(&first_bad, p->d_overflow + 1, 8, cudaMemcpyDeviceToHost, p->st);
-  cudaMemcpyAsync(&overflow, p->d_overflow, 8, cudaMemcpyDeviceToHost, p->st);
-  cudaEventRecord(e1, p->st);
+                    p->d_ra2, p->d_ra2d, p->d_dlen, p->d_overflow, d_exc_tmp,
+                    d_exc_tile_tmp, kExcCap, p->st);
+  unsigned long long counters[3] = {0, 0, 0};  // bad steps, first bad ray, exceptions
+  cudaMemcpyAsync(counters, p->d_overflow, sizeof(counters), cudaMemcpyDeviceToHost, p->st);
   if (cudaStreamSynchronize(p->st) != cudaSuccess) {
     p->err = std::string("matrix construction failed: ") +
              cudaGetErrorString(cudaGetLastError());
     return bail(TG_E_CUDA);
   }
-  if (overflow) {
-    p->err = std::to_string(overflow) +
-             " segments fall outside the two-column pixel window or the "
-             "4-bit step code (first: angle " + std::to_string(first_bad >> 32) +
-             ", column " + std::to_string(first_bad & 0xffffffffull) +
-             "); geometry not supported by this layout";
+  const unsigned long long nexc = counters[2];
+  if (nexc > (unsigned long long)kExcCap) {
+    p->err = std::to_string(nexc) +
+             " segments fall outside their pixel's two-column window (more than " +
+             std::to_string(kExcCap) + "); geometry not supported by this layout";
     return bail(TG_E_GEOMETRY);
   }
+  if (nexc > 0) {
+    // window exceptions as a CSR list over the 8x4 pixel tiles
+    std::vector<int4> ex(nexc);
+    std::vector<int> et(nexc);
+    cudaMemcpy(ex.data(), d_exc_tmp, nexc * sizeof(int4), cudaMemcpyDeviceToHost);
+    cudaMemcpy(et.data(), d_exc_tile_tmp, nexc * sizeof(int), cudaMemcpyDeviceToHost);
+    std::vector<size_t> order(nexc);
+    for (size_t i = 0; i < nexc; ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](size_t u, size_t v) {
+      if (et[u] != et[v]) return et[u] < et[v];
+      if (ex[u].x != ex[v].x) return ex[u].x < ex[v].x;
+      if (ex[u].y != ex[v].y) return ex[u].y < ex[v].y;
+      return ex[u].z < ex[v].z;
+    });
+    std::vector<int> first(M.ntiles + 1, 0);
+    std::vector<int4> sorted(nexc);
+    for (size_t i = 0; i < nexc; ++i) {
+      sorted[i] = ex[order[i]];
+      ++first[et[order[i]] + 1];
+    }
+    for (int t = 0; t < M.ntiles; ++t) first[t + 1] += first[t];
+    if ((rc = dalloc(p, &p->d_exc_first, (size_t)M.ntiles + 1)) ||
+        (rc = dalloc(p, &p->d_exc, (size_t)nexc)))
+      return bail(rc);
+    cudaMemcpyAsync(p->d_exc_first, first.data(), (M.ntiles + 1) * sizeof(int),
+                    cudaMemcpyHostToDevice, p->st);
+    cudaMemcpyAsync(p->d_exc, sorted.data(), nexc * sizeof(int4), cudaMemcpyHostToDevice,
+                    p->st);
+    M.exc_first = p->d_exc_first;
+    M.exc = p->d_exc;
+  }
+  dfree(p, d_exc_tmp, (size_t)kExcCap * sizeof(int4));
+  dfree(p, d_exc_tile_tmp, (size_t)kExcCap * sizeof(int));
+  if (counters[0] && d.delta_index && !otf) {
+    // a stray segment's step does not fit the 4-bit code: this plan's
+    // ray-ordered forward projection traces its rays on the fly instead
+    dfree(p, p->d_rcode, (size_t)words * sizeof(uint32_t));
+    dfree(p, p->d_rstart, (size_t)p->R * sizeof(int));
+    dfree(p, p->d_rlen, (size_t)entries * lbytes);
+    p->d_rcode = nullptr;
+    p->d_rstart = nullptr;
+    p->d_rlen = nullptr;
+    M.rcode = nullptr;
+    M.rstart = nullptr;
+    M.rlen = nullptr;
+    p->info.forward_traced = 1;
+  }
+  launch_weights(G, M, d.mode == TG_MODE_EXACT, p->d_W, p->st);
+  if (p->d_Wh) launch_weights(G, M, 0, p->d_Wh, p->st, true);
+  if (p->fp64) launch_weights64(G, M, p->d_W64, p->st);
+  p->info.window_exceptions = (int64_t)nexc;
+  (void)counters[1];
   if (d.forward_tiles && (rc = build_tiles(p))) {
     if (p->err.empty()) p->err = "building the tile-ordered forward matrix failed";
     return bail(rc);
@@ -710,7 +765,8 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
 
   tg_plan_info& I = p->info;
   I.num_segments = nseg_total;
-  I.forward_bytes = otf ? 0
+  if (otf) I.forward_traced = 1;
+  I.forward_bytes = (otf || p->info.forward_traced) ? 0
                         : entries * (int64_t)lbytes +
                               (d.delta_index ? words * 4 + p->R * 4 : entries * 4);
   I.backward_bytes = (int64_t)dense_n * (int64_t)lbytes;

@@ -42,20 +42,32 @@ __device__ __forceinline__ int tile_of(const DevGeom& G, int ix, int iy,
   return (iy / TS) * tiles_x + ix / TS;
 }
 
+// A 4-bit step code holds (dx, dy) in {0,1} x {-1,0,1}. The reference's
+// tracer can emit a segment far from the previous one (float rounding with
+// the source a million units away, at near-vertical angles on the edge
+// columns): such a step starts a new run, as a tile change does.
+__device__ __forceinline__ bool unit_step(int ix, int iy, int px, int py) {
+  const int dx = ix - px, dy = iy - py;
+  return dx >= 0 && dx <= 1 && dy >= -1 && dy <= 1;
+}
+
 // ---- construction --------------------------------------------------------------
 __global__ void __launch_bounds__(kTraceBlock)
     k_runs_count(DevGeom G, int tiles_x, int* ray_nruns) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= (int64_t)G.P * G.C) return;
   const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
-  int n = 0, cur = -1;
+  int n = 0, cur = -1, px = 0, py = 0;
   const int g = G.C;
   trace_ray(G, a, c, [&](int idx, float, float) {
-    const int t = tile_of(G, idx % g, idx / g, tiles_x);
-    if (t != cur) {
+    const int ix = idx % g, iy = idx / g;
+    const int t = tile_of(G, ix, iy, tiles_x);
+    if (t != cur || !unit_step(ix, iy, px, py)) {
       ++n;
       cur = t;
     }
+    px = ix;
+    py = iy;
   });
   ray_nruns[r] = n;
 }
@@ -81,7 +93,7 @@ __global__ void __launch_bounds__(kTraceBlock)
   const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
   const int g = G.C;
   int64_t i = ray_run_off[r] - 1;
-  int cur = -1, k = -1, len = 0;
+  int cur = -1, k = -1, len = 0, px = 0, py = 0;
   auto close = [&]() {
     if (i >= ray_run_off[r]) {
       run_len[i] = (uint16_t)len;
@@ -91,7 +103,10 @@ __global__ void __launch_bounds__(kTraceBlock)
   trace_ray(G, a, c, [&](int idx, float, float) {
     const int ix = idx % g, iy = idx / g;
     const int t = tile_of(G, ix, iy, tiles_x);
-    if (t != cur) {
+    const bool step_ok = unit_step(ix, iy, px, py);
+    px = ix;
+    py = iy;
+    if (t != cur || !step_ok) {
       close();
       ++i;
       ++k;
@@ -147,7 +162,7 @@ __global__ void __launch_bounds__(kTraceBlock)
   trace_ray(G, a, c, [&](int idx, float l, float) {
     const int ix = idx % g, iy = idx / g;
     const int t = tile_of(G, ix, iy, tiles_x);
-    if (t != cur) {
+    if (t != cur || !unit_step(ix, iy, px, py)) {
       flush();
       ++i;
       cur = t;

@@ -41,7 +41,8 @@ template <bool L16, bool DELTA>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_fill(DevGeom G, MatrixDev M, int ngroups, int* ridx,
                  uint32_t* rcode, int* rstart, void* rlen, float* ra2,
-                 double* ra2d, void* dlen, unsigned long long* overflow) {
+                 double* ra2d, void* dlen, unsigned long long* overflow,
+                 int4* exc, int* exc_tile, int exc_cap) {
   const int grp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (grp >= ngroups) return;
@@ -91,7 +92,15 @@ __global__ void __launch_bounds__(kTraceBlock)
     // backward matrix: slot = column offset inside the pixel's window
     const int slot = c - window_c0(coef, (float)ix, (float)iy);
     if (slot < 0 || slot > 1) {
-      ++bad;
+      // an exception entry (overflow[2] counts them; past the capacity the
+      // plan is refused)
+      int tile, tl;
+      pixel_tile(ix, iy, M.tiles_x, &tile, &tl);
+      const unsigned long long k = atomicAdd(overflow + 2, 1ull);
+      if (k < (unsigned long long)exc_cap) {
+        exc[k] = make_int4(tl, a, c, __float_as_int(l));
+        exc_tile[k] = tile;
+      }
     } else {
       // A present entry never stores +0: a zero length is kept as -0 so the
       // backprojection still visits it (0 * a non-finite factor is NaN in
@@ -117,7 +126,7 @@ __global__ void __launch_bounds__(kTraceBlock)
     rcode[cbase + (int64_t)(s >> 3) * 32] = word;
   ra2[r] = a2;
   if (ra2d) ra2d[r] = a2d;
-  if (bad) {
+  if (bad) {  // step codes that do not fit 4 bits
     atomicAdd(overflow, bad);
     // the first offending ray (lowest angle, then column) for the message
     atomicMin(overflow + 1, ((unsigned long long)a << 32) | (unsigned)c);
@@ -169,6 +178,16 @@ __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W) {
       sum = tk;
     }
   }
+  for_each_exception(M, tile, lane, [&](float l, int, int) {
+    if constexpr (HALF) l = __half2float(__float2half_rn(l));
+    if (exact) {
+      sum = fadd(sum, l);
+    } else {
+      const float yk = l - comp, tk = sum + yk;
+      comp = (tk - sum) - yk;
+      sum = tk;
+    }
+  });
   W[p] = sum;
 }
 
@@ -200,23 +219,27 @@ void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
 void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
                        uint32_t* rcode, int* rstart, void* rlen, float* ra2,
                        double* ra2d, void* dlen, unsigned long long* overflow,
-                       cudaStream_t st) {
+                       int4* exc, int* exc_tile, int exc_cap, cudaStream_t st) {
   const int ngroups = G.P * G.gpa;
   const int blocks = (ngroups * 32 + kTraceBlock - 1) / kTraceBlock;
   const bool l16 = M.len_kind != LK_F32;
   const bool delta = rcode != nullptr;
   if (l16 && delta)
     k_trace_fill<true, true><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow);
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow, exc,
+        exc_tile, exc_cap);
   else if (l16)
     k_trace_fill<true, false><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow);
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow, exc,
+        exc_tile, exc_cap);
   else if (delta)
     k_trace_fill<false, true><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow);
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow, exc,
+        exc_tile, exc_cap);
   else
     k_trace_fill<false, false><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow);
+        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow, exc,
+        exc_tile, exc_cap);
 }
 
 void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
