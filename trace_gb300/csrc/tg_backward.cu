@@ -33,6 +33,9 @@ constexpr int kCoefChunk = 512;  // angles of window coefficients per stage
 // a thread at 5): at 6 the 8-slice variants spill inside the angle loop.
 constexpr int kMinBlocks = 5;
 constexpr int kMinBlocks16 = 4;  // 16 slices per pass: 16 accumulators more
+// half factors + penalty: the mixed-precision FMAs need no converted floats,
+// 40 registers suffice (6 blocks per SM hide more of the gather latency)
+constexpr int kMinBlocksHalfPen = 6;
 
 // Four angles of one lane's backward-matrix entries: 16 bytes for 16-bit
 // codes (two per angle), 32 bytes for floats. The entries of angles
@@ -144,7 +147,7 @@ __device__ __forceinline__ void accumulate(float (&acc)[K], const float (&rf)[K]
 }
 
 template <int K, int LK, bool EXACT, bool PEN, bool FH>
-__global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
+__global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : ((FH && PEN) ? kMinBlocksHalfPen : kMinBlocks))
     k_backward(IterArgs A, int batch, const float* __restrict__ cur,
                float* __restrict__ next, const float* __restrict__ upd,
                float* __restrict__ rep_num, int epi) {
