@@ -181,8 +181,13 @@ int trace_ray(const Geometry& G, int p, int c, TraceWs& ws, Emit&& emit) {
         sg.dlen2 = ddx * ddx + ddy * ddy;
         sg.dlen = std::sqrt(sg.dlen2);
       }
-      emit(sg);
-      ++nseg;
+      // A stray segment whose cell index falls outside the grid (the
+      // reference would index its arrays out of bounds: undefined) is
+      // dropped; in-grid indices are kept as the reference forms them.
+      if (sg.idx >= 0 && sg.idx < g * g) {
+        emit(sg);
+        ++nseg;
+      }
     }
     px = x;
     py = y;
@@ -247,7 +252,16 @@ int trace_ray_arrays(const Geometry& G, int p, int c, TraceWs& ws) {
     ln[i] = std::sqrt(ln2[i]);
     ix[i] = (int)(midx + mg) + (int)(midy + mg) * g;
   }
-  return nseg;
+  // drop stray segments outside the grid, as trace_ray does (rare)
+  int kept = 0;
+  for (int i = 0; i < nseg; ++i) {
+    if (ix[i] < 0 || ix[i] >= g * g) continue;
+    ix[kept] = ix[i];
+    ln[kept] = ln[i];
+    ln2[kept] = ln2[i];
+    ++kept;
+  }
+  return kept;
 }
 
 template <class F>

@@ -41,7 +41,7 @@ __device__ __forceinline__ float grid_line(const DevGeom& G, int n) {
 
 // Streams the segments of ray (a, c) to emit(idx, len, len2) in the order of
 // the reference tracer (trace_utils.cc:48-216 composed as sirt.cc:126-160).
-// Returns the segment count max(len-1, 0).
+// Returns the number of segments emitted.
 //
 // Crossings with horizontal grid lines ("a" points) and vertical grid lines
 // ("b" points) are walked by two cursors that skip crossings outside the
@@ -108,8 +108,13 @@ __device__ __forceinline__ int trace_ray(const DevGeom& G, int a, int c,
       const float len = fsqrt(len2);
       const int ix = __float2int_rz(fadd(midx, G.mgrids));
       const int iy = __float2int_rz(fadd(midy, G.mgrids));
-      emit(ix + iy * g, len, len2);
-      ++nseg;
+      const int idx = ix + iy * g;
+      // A stray segment whose cell index falls outside the grid (the
+      // reference indexes its arrays out of bounds there) is dropped.
+      if ((unsigned)idx < (unsigned)g * (unsigned)g) {
+        emit(idx, len, len2);
+        ++nseg;
+      }
     }
     px = x;
     py = y;
