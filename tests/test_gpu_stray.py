@@ -74,3 +74,26 @@ def test_fast_paths_with_stray_segments_against_fp64(data, alg):
         plan.iterate(alg, 3, tg.default_params(alg, beta=0.1))
         assert rel_l2(plan.get_recon(alg), ref) < 1e-4, kw
         plan.close()
+
+
+def test_out_of_grid_stray_segment_is_dropped():
+    """At 2048 columns x 1065 angles the reference's tracer gives the last
+    angle's edge ray a 1/16-long segment whose cell index is one row past
+    the grid (the reference would index out of bounds). Both the device
+    tracer and the oracle drop it; everything else matches."""
+    C2, P2 = 2048, 1065
+    th = theta_uniform(P2)
+    tabs = O.angle_table(th)
+    counts, offs, idx, ln, _, _ = O.ref_trace(C2, th[[P2 - 1]]) if O.ref() else (None,) * 6
+    if idx is not None:
+        assert ((idx < 0) | (idx >= C2 * C2)).sum() == 1
+    from trace_gb300.phantom import ellipse_phantoms
+    ph = ellipse_phantoms(C2, 1, seed=43)
+    sino = O.forward(ph, tabs, threads=16)
+    plan = tg.Plan(P2, 1, C2, th)
+    cnt = plan.trace_rays(counts_only=True)
+    ocnt, *_ = O.trace(C2, tuple(t[P2 - 1:] for t in tabs), threads=8)
+    assert np.array_equal(cnt[(P2 - 1) * C2:], ocnt)
+    plan.set_recon("sirt", ph)
+    assert np.array_equal(bits(plan.forward_project("sirt")), bits(sino))
+    plan.close()

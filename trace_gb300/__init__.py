@@ -292,11 +292,14 @@ class Plan:
         self._chk(self._lib.tg_forward_project(self._h, self._alg(alg), C.byref(p), _ptr(out), 0))
         return out
 
-    def trace_rays(self):
-        """(counts, offsets, idx, len, len2) of every ray, r = p*C + c."""
+    def trace_rays(self, counts_only=False):
+        """(counts, offsets, idx, len, len2) of every ray, r = p*C + c;
+        counts_only: just the per-ray segment counts."""
         R = self.P * self.C
         counts = np.empty(R, np.int32)
         self._chk(self._lib.tg_trace_rays(self._h, _ptr(counts), None, None, None, None))
+        if counts_only:
+            return counts
         offs = np.zeros(R + 1, np.int64)
         np.cumsum(counts, out=offs[1:])
         n = int(offs[-1])
