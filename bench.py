@@ -419,7 +419,8 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
         tp.forward_project("sirt", out=sample)
         tp.close()
         best, res = autotune(theta, sample, alg, prm, len_storage=args.len_storage,
-                             stream=stream)
+                             stream=stream,
+                             fixed={"half_gathers": True} if args.half else None)
         K, args.tiles, args.staged = (best["slices_per_pass"], best["forward_tiles"],
                                       best["backward_staged"])
         args.otf = best.get("forward_on_the_fly", False)
