@@ -494,15 +494,16 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
         },
     }
 
+    recon_bytes = 4 * S * C * C
+    sino_bytes = 4 * P * S * C
+    plan.close()  # before the comparison plans (a full volume holds ~200 GB)
+    del plan
+    torch.cuda.empty_cache()
+
     # relative L2 against an FP64 run on a slice subset
     rel = None
     if args.fp64_check and rank == 0:
         rel = fp64_check(args, W, theta, sino, prm, tg, torch, dev)
-
-    recon_bytes = 4 * S * C * C
-    sino_bytes = 4 * P * S * C
-    plan.close()
-    del plan
 
     # ---- plain FP32 path (f32 lengths, 1 slice per pass, reference op order)
     plain = None
