@@ -33,9 +33,6 @@ constexpr int kCoefChunk = 512;  // angles of window coefficients per stage
 // a thread at 5): at 6 the 8-slice variants spill inside the angle loop.
 constexpr int kMinBlocks = 5;
 constexpr int kMinBlocks16 = 4;  // 16 slices per pass: 16 accumulators more
-// half factors + penalty: the mixed-precision FMAs need no converted floats,
-// 40 registers suffice (6 blocks per SM hide more of the gather latency)
-constexpr int kMinBlocksHalfPen = 6;
 
 // Four angles of one lane's backward-matrix entries: 16 bytes for 16-bit
 // codes (two per angle), 32 bytes for floats. The entries of angles
@@ -122,6 +119,20 @@ __device__ __forceinline__ void fma_halves(float (&acc)[K], float l, const __hal
   }
 }
 
+// K halves as K/2 32-bit words (one aligned load), for the pipelined loop.
+template <int K>
+__device__ __forceinline__ void load_hwords(uint32_t (&w)[K / 2], const __half* p) {
+  if constexpr (K == 2) {
+    w[0] = __ldg(reinterpret_cast<const unsigned int*>(p));
+  } else if constexpr (K == 4) {
+    const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
+    w[0] = v.x; w[1] = v.y;
+  } else {
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
+    w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+  }
+}
+
 // FH: the factors are halves (factor - 1), see k_fwd_finish; the missing
 // sum of lengths is the pixel's total length W, added in the epilogue.
 template <int K, bool EXACT, bool PEN, bool FH>
@@ -147,7 +158,7 @@ __device__ __forceinline__ void accumulate(float (&acc)[K], const float (&rf)[K]
 }
 
 template <int K, int LK, bool EXACT, bool PEN, bool FH>
-__global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : ((FH && PEN) ? kMinBlocksHalfPen : kMinBlocks))
+__global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
     k_backward(IterArgs A, int batch, const float* __restrict__ cur,
                float* __restrict__ next, const float* __restrict__ upd,
                float* __restrict__ rep_num, int epi) {
@@ -197,6 +208,42 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : ((FH && PEN) 
     for (int a4 = 0; a4 < na; a4 += 4) {
       Quad<LK> nq;
       if (a4 + 4 < na) load_quad<LK>(qp + qstep, nq);
+      if constexpr (FH && !EXACT && K >= 2 && K <= 8) {
+        // software pipeline over the quad's 4 angles: the factor loads of
+        // angle j + 1 are in flight while angle j's FMAs run
+        uint32_t w0[2][K / 2], w1[2][K / 2];
+        unsigned short lh0[2], lh1[2];
+        auto issue = [&](int j, int b) {
+          float l0, l1;
+          bool h0, h1;
+          quad_pair<LK, false>(q, j, A.M.inv_scale, l0, l1, h0, h1);
+          const int c0 = window_c0(s_coef[a4 + j], xf, yf);
+          const __half* hb = reinterpret_cast<const __half*>(ua) + j * ck + c0 * K;
+          lh0[b] = __half_as_ushort(__float2half_rn(l0));
+          lh1[b] = __half_as_ushort(__float2half_rn(l1));
+#pragma unroll
+          for (int i = 0; i < K / 2; ++i) { w0[b][i] = 0u; w1[b][i] = 0u; }
+          if (h0) load_hwords<K>(w0[b], hb);
+          if (h1) load_hwords<K>(w1[b], hb + K);
+        };
+        auto consume = [&](int b) {
+#pragma unroll
+          for (int i = 0; i < K / 2; ++i) {
+            asm("{ .reg .b16 lo, hi; mov.b32 {lo, hi}, %2; fma.rn.f32.f16 %0, lo, %3, %0;"
+                " fma.rn.f32.f16 %1, hi, %3, %1; }"
+                : "+f"(acc[2 * i]), "+f"(acc[2 * i + 1]) : "r"(w0[b][i]), "h"(lh0[b]));
+            asm("{ .reg .b16 lo, hi; mov.b32 {lo, hi}, %2; fma.rn.f32.f16 %0, lo, %3, %0;"
+                " fma.rn.f32.f16 %1, hi, %3, %1; }"
+                : "+f"(acc[2 * i]), "+f"(acc[2 * i + 1]) : "r"(w1[b][i]), "h"(lh1[b]));
+          }
+        };
+        issue(0, 0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (j < 3) issue(j + 1, (j + 1) & 1);
+          consume(j & 1);
+        }
+      } else
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         float l0, l1;
