@@ -340,12 +340,14 @@ __device__ __forceinline__ float chunk_len(const Chunk<LK>& ch, int j,
 
 template <int K, int LK, bool H>
 __global__ void __launch_bounds__(kBlock)
-    k_forward_tiled(TileMatrixDev T, int g, float inv_scale,
+    k_forward_tiled(TileMatrixDev T, int g, float inv_scale, int splits,
                     const float* __restrict__ recon, float* __restrict__ sim) {
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   __half* smh = reinterpret_cast<__half*>(smem4);
-  const int t = blockIdx.x;
+  // `splits` blocks share a tile (small grids: fewer tiles than SMs); each
+  // loads the tile and takes every splits-th warp group
+  const int t = blockIdx.x / splits, part = blockIdx.x - t * splits;
   const int x0 = (t % T.tiles_x) * TS, y0 = (t / T.tiles_x) * TS;
   if constexpr (H)
     tile_load_half<K>(smh, recon, g, x0, y0);
@@ -354,7 +356,7 @@ __global__ void __launch_bounds__(kBlock)
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g0 = T.group_first[t], g1 = T.group_first[t + 1];
-  for (int grp = g0 + warp; grp < g1; grp += kBlock / 32) {
+  for (int grp = g0 + part * (kBlock / 32) + warp; grp < g1; grp += splits * (kBlock / 32)) {
     const int slot = grp * 32 + lane;
     const int ray = T.gray[slot];
     const int n = T.glen[slot];
@@ -434,7 +436,13 @@ void fwd_tiled_launch(const TileMatrixDev& T, int g, float inv_scale,
   const int smem = TilePlanes<K, H>::kBytes;
   cudaFuncSetAttribute(k_forward_tiled<K, LK, H>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  k_forward_tiled<K, LK, H><<<T.ntiles, kBlock, smem, st>>>(T, g, inv_scale, recon, sim);
+  // at least two blocks per SM when the grid has few tiles
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int splits = max(1, min(16, (2 * sms + T.ntiles - 1) / T.ntiles));
+  k_forward_tiled<K, LK, H><<<T.ntiles * splits, kBlock, smem, st>>>(T, g, inv_scale, splits,
+                                                                     recon, sim);
 }
 
 template <int K, bool H>
