@@ -97,3 +97,14 @@ def test_out_of_grid_stray_segment_is_dropped():
     plan.set_recon("sirt", ph)
     assert np.array_equal(bits(plan.forward_project("sirt")), bits(sino))
     plan.close()
+
+
+def test_fp64_mode_with_stray_segments(data):
+    th, tabs, _, sino = data
+    ref = O.run("sirt", sino, tables=tabs, n_iter=2, precision=O.F64, threads=16)["recon"]
+    plan = tg.Plan(P, 1, C, th, mode="fp64")
+    plan.set_sinogram(sino)
+    plan.reset_recon("sirt")
+    plan.iterate("sirt", 2)
+    assert rel_l2(plan.get_recon("sirt"), ref) < 1e-6
+    plan.close()
