@@ -561,9 +561,11 @@ def fp64_check(args, W, theta, sino, prm, tg, torch, dev):
     sub = sino[:, :n, :].contiguous()
     configs = {
         "fp64": dict(len_storage="f32", mode="fp64"),
+        # the measured configuration, same kernels (same slices per pass: the
+        # subset fills part of one batch)
         "mixed": dict(len_storage=args.len_storage, mode="fast", delta_index=True,
                       forward_tiles=args.tiles, backward_staged=args.staged,
-                      half_gathers=args.half),
+                      half_gathers=args.half, slices_per_pass=args.slices_per_pass),
         "plain_fp32": dict(len_storage="f32", mode="exact"),
     }
     runs = {}
