@@ -226,11 +226,23 @@ def barrier(ws):
 
 
 # ---------------------------------------------------------------------------
+# The reference builds MLEM and APMLR with -ffast-math (src/mlem/Makefile:11,
+# src/apmlr/Makefile:11), SIRT and PML without: the CPU baseline times the
+# port with the same choice.
+FAST_MATH_ALGS = ("mlem", "apmlr")
+
+
+def cpu_flags(alg):
+    return "-O3 -ffast-math" if alg in FAST_MATH_ALGS else "-O3 (strict IEEE)"
+
+
 def oracle_iteration(W, tabs, sino, threads):
     from oracle import oracle as O
     kw = {"beta": W["beta"]} if W["alg"] in ("pml", "apmlr") else {}
-    O.run(W["alg"], sino, tables=tabs, n_iter=1, threads=threads, apply_abs=0, **kw)
-    return O.port().tor_last_loop_seconds()
+    fm = W["alg"] in FAST_MATH_ALGS
+    O.run(W["alg"], sino, tables=tabs, n_iter=1, threads=threads, apply_abs=0,
+          fast_math=fm, **kw)
+    return O.port(fm).tor_last_loop_seconds()
 
 
 def cpu_baseline(W, steps=1, threads=None):
@@ -244,7 +256,7 @@ def cpu_baseline(W, steps=1, threads=None):
             "cores": threads, "kind": "port",
             "sample": f"1 slice x 1 {W['alg'].upper()} iteration at {C}x{C}, {P} "
                       f"angles ({threads} threads, replicas + tree merge as the "
-                      f"reference engine); median of {steps}",
+                      f"reference engine, {cpu_flags(W['alg'])}); median of {steps}",
             "seconds": secs}
 
 
@@ -267,7 +279,8 @@ def run_reference(args, W):
             oracle_iteration(W, tabs, sino, threads)
         secs = [oracle_iteration(W, tabs, sino, threads) for _ in range(args.steps)]
         sample = (f"1 slice x 1 {W['alg'].upper()} iteration per step at the workload "
-                  "geometry (oracle port of the reference's threaded CPU path)")
+                  "geometry (oracle port of the reference's threaded CPU path, "
+                  f"{cpu_flags(W['alg'])} as the reference builds it)")
     total = sum(secs)
     val = len(secs) / total
     line = {
@@ -817,8 +830,9 @@ def batch_cpu_baseline(W, probs, sample=4):
         sino = O.forward(ellipse_phantoms(pr["C"], 1, seed=1000 + i), tabs, threads=threads)
         if pr["alg"] != "sirt":
             sino = np.abs(sino)
-        O.run(pr["alg"], sino, tables=tabs, n_iter=1, threads=threads)
-        secs += O.port().tor_last_loop_seconds()
+        fm = pr["alg"] in FAST_MATH_ALGS
+        O.run(pr["alg"], sino, tables=tabs, n_iter=1, threads=threads, fast_math=fm)
+        secs += O.port(fm).tor_last_loop_seconds()
     return {"value": sample / secs, "unit": "slice-iter/s", "cores": threads,
             "kind": "port", "seconds": secs, "slice_iters": sample,
             "sample": "1 slice-iteration of each of the problems " + ", ".join(

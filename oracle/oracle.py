@@ -19,6 +19,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
+# the same port built with -ffast-math (the reference's MLEM/APMLR flags):
+# for timing the CPU baseline only
+PORT_FAST_SO = os.path.join(HERE, "_build", "liboracle_fastmath.so")
 REF_SO = os.path.join(HERE, "_ref", "libtrace_ref.so")
 REF_SRC = os.environ.get("TRACE_REFERENCE_DIR", "/root/reference")
 
@@ -28,7 +31,7 @@ F32, F64 = 0, 1
 
 
 def build_port(quiet: bool = True) -> str:
-    subprocess.run(["make", "-s", "port"], cwd=HERE, check=True,
+    subprocess.run(["make", "-s", "-j2", "port"], cwd=HERE, check=True,
                    stdout=subprocess.DEVNULL if quiet else None)
     return PORT_SO
 
@@ -63,19 +66,21 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
-_port = None
+_port = {}
 _ref = None
 
 
-def port():
-    global _port
-    if _port is None:
-        if not os.path.exists(PORT_SO):
+def port(fast_math=False):
+    """The oracle library; fast_math: the -ffast-math build (timing only)."""
+    if fast_math not in _port:
+        path = PORT_FAST_SO if fast_math else PORT_SO
+        if not os.path.exists(path):
             build_port()
-        _port = C.CDLL(PORT_SO)
-        _port.tor_run.argtypes = [C.POINTER(_RunArgs)]
-        _port.tor_last_loop_seconds.restype = C.c_double
-    return _port
+        lib = C.CDLL(path)
+        lib.tor_run.argtypes = [C.POINTER(_RunArgs)]
+        lib.tor_last_loop_seconds.restype = C.c_double
+        _port[fast_math] = lib
+    return _port[fast_math]
 
 
 def ref():
@@ -132,8 +137,11 @@ def trace(num_cols, tables, center=0.0, threads=8):
 def run(alg, sino, theta=None, tables=None, *, n_iter=1, precision=F32, dlen=0,
         center=0.0, threads=1, beta=10.0, beta1=1.0, delta=1.0, delta1=1.0,
         regw=1.0, slice_id=0, num_total_slices=None, apply_abs=None,
-        apmlr_fixed=0, recon_in=None, want_iters=False, want_replica=False):
-    """Oracle reconstruction. sino is [P][S][C] float32.
+        apmlr_fixed=0, recon_in=None, want_iters=False, want_replica=False,
+        fast_math=False):
+    """Oracle reconstruction. sino is [P][S][C] float32. fast_math: run the
+    -ffast-math build (timing the reference's MLEM/APMLR flags; results are
+    not the reference's arithmetic).
 
     Returns dict(recon, iters, replica, seconds). recon has S + 2*halo
     slices (halo = 1 for APMLR)."""
@@ -171,11 +179,12 @@ def run(alg, sino, theta=None, tables=None, *, n_iter=1, precision=F32, dlen=0,
         keep.append(recon_in)
         a.recon_in = _ptr(recon_in)
     a.recon_out, a.iters_out, a.replica_out = _ptr(out), _ptr(iters), _ptr(rep)
-    rc = port().tor_run(C.byref(a))
+    L = port(fast_math)
+    rc = L.tor_run(C.byref(a))
     if rc != 0:
         raise ValueError(f"tor_run failed with status {rc}")
     return {"recon": out, "iters": iters, "replica": rep,
-            "seconds": port().tor_last_loop_seconds()}
+            "seconds": L.tor_last_loop_seconds()}
 
 
 # ---- the compiled reference -------------------------------------------------
