@@ -66,13 +66,16 @@ def test_on_the_fly_operator_path_and_memory():
 
 
 def test_on_the_fly_with_tiles_and_half_gathers():
+    """The tile stream is built from the stored delta-coded matrix, the stored
+    explicit-index matrix, or by tracing (no stored matrix): all three give
+    the same reconstruction."""
     C, P, S = 96, 72, 8
     th, tabs, _, sino = ellipse_sino(C, P, S, seed=13)
     prm = tg.default_params("pml", beta=0.05)
     outs = []
-    for otf in (False, True):
+    for delta, otf in ((True, False), (True, True), (False, False)):
         plan = tg.Plan(P, S, C, th, slices_per_pass=8, mode="fast", len_storage="u16",
-                       delta_index=True, forward_tiles=True, half_gathers=True,
+                       delta_index=delta, forward_tiles=True, half_gathers=True,
                        forward_on_the_fly=otf)
         plan.set_sinogram(sino, apply_abs=True)
         plan.reset_recon("pml")
@@ -81,6 +84,7 @@ def test_on_the_fly_with_tiles_and_half_gathers():
         plan.close()
     # the tiled forward's run sums are added atomically: order may differ
     assert rel_l2(outs[1], outs[0]) < 1e-6
+    assert rel_l2(outs[2], outs[0]) < 1e-6
 
 
 def test_on_the_fly_rejected_in_fp64_mode():

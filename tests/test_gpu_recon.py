@@ -224,3 +224,26 @@ def test_sinogram_clip_matches_oracle_on_clipped_input(on_device):
     plan.iterate("mlem", 4)
     assert rel_l2(plan.get_recon("mlem"), ref) < 2e-6
     plan.close()
+
+
+def test_get_recon_into_host_buffers():
+    """get_recon writes into a caller's host buffer (numpy or pinned CPU
+    tensor) with the same bits as a fresh download, and rejects a buffer of
+    the wrong shape or type."""
+    torch = pytest.importorskip("torch")
+    f = golden("recon_apmlr.npz")
+    plan = plan_for(f, slices_per_pass=2)
+    alg = load(plan, f)
+    plan.iterate(alg, 2, params_of(f))
+    want = plan.get_recon(alg)
+    host = np.empty_like(want)
+    assert plan.get_recon(alg, out=host) is host
+    pinned = torch.empty(want.shape, dtype=torch.float32).pin_memory()
+    plan.get_recon(alg, out=pinned)
+    assert np.array_equal(bits(host), bits(want))
+    assert np.array_equal(bits(pinned.numpy()), bits(want))
+    with pytest.raises(ValueError):
+        plan.get_recon(alg, out=np.empty(want.shape[1:], np.float32))
+    with pytest.raises(ValueError):
+        plan.get_recon(alg, out=np.empty(want.shape, np.float64))
+    plan.close()

@@ -109,7 +109,7 @@ def _ptr(a):
         return None
     if isinstance(a, np.ndarray):
         return a.ctypes.data_as(C.c_void_p)
-    if hasattr(a, "data_ptr"):  # torch tensor on the device
+    if hasattr(a, "data_ptr"):  # torch tensor (device or host)
         return C.c_void_p(a.data_ptr())
     return C.c_void_p(int(a))
 
@@ -244,11 +244,21 @@ class Plan:
         self._chk(self._lib.tg_set_recon(self._h, self._alg(alg), _ptr(recon), 0))
 
     def get_recon(self, alg, out=None):
+        """Download the reconstruction ([S + 2 halo][C][C]) into `out` (a
+        device tensor, or a host array / CPU tensor, e.g. pinned, that must be
+        float32, C-contiguous and of that shape) or into a new host array."""
         if out is not None and _is_device(out):
             self._chk(self._lib.tg_get_recon(self._h, self._alg(alg), _ptr(out), 1))
             return out
         n = self.S + 2 * self.halo(alg)
-        out = np.empty((n, self.C, self.C), np.float32)
+        if out is None:
+            out = np.empty((n, self.C, self.C), np.float32)
+        else:
+            view = out.numpy() if hasattr(out, "numpy") else out
+            if (not isinstance(view, np.ndarray) or view.dtype != np.float32
+                    or view.shape != (n, self.C, self.C) or not view.flags.c_contiguous):
+                raise ValueError(f"out must be a C-contiguous float32 array of shape "
+                                 f"{(n, self.C, self.C)}")
         self._chk(self._lib.tg_get_recon(self._h, self._alg(alg), _ptr(out), 0))
         return out
 

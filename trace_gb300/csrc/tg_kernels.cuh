@@ -44,6 +44,19 @@ struct MatrixDev {
 // Tile-staged forward matrix (tg_tiles.cu): per 64x64 tile, groups of 32
 // runs (consecutive segments of one ray inside the tile), lane = run.
 constexpr int kTileSide = 64;
+
+__device__ __forceinline__ int tile_of_pixel(int ix, int iy, int tiles_x) {
+  return (iy / kTileSide) * tiles_x + ix / kTileSide;
+}
+
+// A 4-bit step code holds (dx, dy) in {0,1} x {-1,0,1}. The reference's
+// tracer can emit a segment far from the previous one (float rounding with
+// the source a million units away, at near-vertical angles on the edge
+// columns): such a step starts a new run, as a tile change does.
+__device__ __forceinline__ bool unit_step(int ix, int iy, int px, int py) {
+  const int dx = ix - px, dy = iy - py;
+  return dx >= 0 && dx <= 1 && dy >= -1 && dy <= 1;
+}
 struct TileMatrixDev {
   int tiles_x, ntiles;
   const int* group_first;   // [ntiles + 1] first group of each tile
@@ -106,8 +119,11 @@ __device__ __forceinline__ void apmlr_axial(const IterArgs& A, int s, int* up,
 }
 
 // tg_trace.cu
+// ray_nruns (optional): runs per ray of the tile-ordered forward matrix
+// (a new run at each tile change and non-unit step), counted in the same pass
 void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
-                        unsigned* maxlen_bits, cudaStream_t st);
+                        unsigned* maxlen_bits, int tiles_x, int* ray_nruns,
+                        cudaStream_t st);
 void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
                        uint32_t* rcode, int* rstart, void* rlen, float* ra2,
                        double* ra2d, void* dlen, unsigned long long* overflow,
@@ -155,17 +171,18 @@ void launch_convert(const float* in, double* out, int64_t n, cudaStream_t st);
 void launch_narrow(const double* in, float* out, int64_t n, cudaStream_t st);
 void launch_fill64(double* p, int64_t n, double v, cudaStream_t st);
 // tg_tiles.cu
-void launch_runs_count(const DevGeom& G, int tiles_x, int* ray_nruns,
-                       cudaStream_t st);
 // Run sort key: tile | chunk-count class | ray | ordinal (RunKey).
 struct RunKey {
   int ray_bits;  // bits of the ray id field
   __host__ __device__ int class_shift() const { return 8 + ray_bits; }
   __host__ __device__ int tile_shift() const { return 13 + ray_bits; }
 };
-void launch_runs_emit(const DevGeom& G, int tiles_x, RunKey rk, const int64_t* ray_run_off,
-                      unsigned long long* key, int* val, uint16_t* run_lp,
-                      uint16_t* run_len, int* tile_count, cudaStream_t st);
+// Run emission and the tile-stream fill read each ray's segments back from
+// the ray-ordered forward matrix M when it is stored (M.rlen), else trace them.
+void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, RunKey rk,
+                      const int64_t* ray_run_off, unsigned long long* key, int* val,
+                      uint16_t* run_lp, uint16_t* run_len, int* tile_count,
+                      cudaStream_t st);
 int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
               int* val_in, int* val_out, int64_t n, int end_bit,
               cudaStream_t st);
@@ -175,7 +192,7 @@ void launch_runs_group(RunKey rk, const unsigned long long* skey, const int* sva
                        const uint16_t* run_len, int* gray, uint16_t* glp,
                        uint16_t* glen, int* gsteps, int* run_slot,
                        cudaStream_t st);
-void launch_runs_fill(const DevGeom& G, int tiles_x, int len_kind, float scale,
+void launch_runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x,
                       const int64_t* ray_run_off, const int* run_slot,
                       const int64_t* gseg_off, const int64_t* gcode_off,
                       void* tlen, uint32_t* tcode, cudaStream_t st);

@@ -291,7 +291,7 @@ float* batch_ptr(tg_plan* p, float* base, int batch_slot) {
 
 // Tile-ordered forward matrix (tg_tiles.cu): runs of each ray inside 64x64
 // tiles, sorted by (tile, chunk-count class, ray) and packed 32 per warp group.
-int build_tiles(tg_plan* p) {
+int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
   const DevGeom& G = p->G;
   const int C = p->C;
   const int tiles_x = (C + kTileSide - 1) / kTileSide;
@@ -313,13 +313,7 @@ int build_tiles(tg_plan* p) {
     for (auto& t : tmp) dfree(p, t.first, t.second);
     tmp.clear();
   };
-  int* ray_nruns = nullptr;
-  int rc = talloc(&ray_nruns, (size_t)p->R, false);
-  if (rc) return release(), rc;
-  launch_runs_count(G, tiles_x, ray_nruns, p->st);
-  std::vector<int> nruns(p->R);
-  cudaMemcpyAsync(nruns.data(), ray_nruns, p->R * 4, cudaMemcpyDeviceToHost, p->st);
-  if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run count failed");
+  int rc = TG_OK;
   std::vector<int64_t> run_off(p->R);
   int64_t NR = 0;
   for (int64_t r = 0; r < p->R; ++r) {
@@ -338,7 +332,8 @@ int build_tiles(tg_plan* p) {
       (rc = talloc(&tile_count, (size_t)ntiles, true)))
     return release(), rc;
   cudaMemcpyAsync(d_run_off, run_off.data(), p->R * 8, cudaMemcpyHostToDevice, p->st);
-  launch_runs_emit(G, tiles_x, rk, d_run_off, key, val, run_lp, run_len, tile_count, p->st);
+  launch_runs_emit(G, p->M, tiles_x, rk, d_run_off, key, val, run_lp, run_len, tile_count,
+                   p->st);
   if (sort_runs(key, key2, val, val2, NR, end_bit, p->st))
     return release(), fail(p, TG_E_CUDA, "sorting the tile runs failed");
   std::vector<int> tcount(ntiles);
@@ -399,8 +394,8 @@ int build_tiles(tg_plan* p) {
   }
   cudaMemcpyAsync(d_seg_off, seg_off.data(), groups * 8, cudaMemcpyHostToDevice, p->st);
   cudaMemcpyAsync(d_code_off, code_off.data(), groups * 8, cudaMemcpyHostToDevice, p->st);
-  launch_runs_fill(G, tiles_x, p->len_kind, p->M.scale, d_run_off, run_slot, d_seg_off,
-                   d_code_off, tlen, tcode, p->st);
+  launch_runs_fill(G, p->M, tiles_x, d_run_off, run_slot, d_seg_off, d_code_off, tlen,
+                   tcode, p->st);
   if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run fill failed");
   release();
   if ((rc = dalloc(p, &p->d_sim, (size_t)p->R * p->K, true))) return rc;
@@ -576,14 +571,26 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
       (rc = dalloc(p, &p->d_maxlen, 1, true)) ||
       (rc = dalloc(p, &p->d_overflow, 3, true)))
     return bail(rc);
-  launch_trace_count(G, p->d_rnseg, p->d_rcap, p->d_maxlen, p->st);
+  // runs per ray of the tile-ordered forward matrix, counted in the same pass
+  int* d_nruns = nullptr;
+  std::vector<int> h_nruns;
+  if (d.forward_tiles) {
+    if ((rc = dalloc(p, &d_nruns, (size_t)p->R))) return bail(rc);
+    h_nruns.resize(p->R);
+  }
+  launch_trace_count(G, p->d_rnseg, p->d_rcap, p->d_maxlen,
+                     (C + kTileSide - 1) / kTileSide, d_nruns, p->st);
+  if (d_nruns)
+    cudaMemcpyAsync(h_nruns.data(), d_nruns, p->R * 4, cudaMemcpyDeviceToHost, p->st);
   std::vector<int> rcap(ngroups);
   unsigned maxbits = 0;
   p->h_nseg.resize(p->R);
   cudaMemcpyAsync(rcap.data(), p->d_rcap, ngroups * 4, cudaMemcpyDeviceToHost, p->st);
   cudaMemcpyAsync(&maxbits, p->d_maxlen, 4, cudaMemcpyDeviceToHost, p->st);
   cudaMemcpyAsync(p->h_nseg.data(), p->d_rnseg, p->R * 4, cudaMemcpyDeviceToHost, p->st);
-  if (cudaStreamSynchronize(p->st) != cudaSuccess) {
+  const cudaError_t traced = cudaStreamSynchronize(p->st);
+  if (d_nruns) dfree(p, d_nruns, (size_t)p->R * sizeof(int));
+  if (traced != cudaSuccess) {
     p->err = std::string("tracing failed: ") + cudaGetErrorString(cudaGetLastError());
     return bail(TG_E_CUDA);
   }
@@ -743,7 +750,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   if (p->fp64) launch_weights64(G, M, p->d_W64, p->st);
   p->info.window_exceptions = (int64_t)nexc;
   (void)counters[1];
-  if (d.forward_tiles && (rc = build_tiles(p))) {
+  if (d.forward_tiles && (rc = build_tiles(p, h_nruns))) {
     if (p->err.empty()) p->err = "building the tile-ordered forward matrix failed";
     return bail(rc);
   }

@@ -37,39 +37,52 @@ constexpr int kTraceBlock = 128;
 // steps past a run's end, empty lanes), with a zero length.
 constexpr uint32_t kStayWord = 0x22222222u;
 
-__device__ __forceinline__ int tile_of(const DevGeom& G, int ix, int iy,
-                                       int tiles_x) {
-  return (iy / TS) * tiles_x + ix / TS;
+__device__ __forceinline__ int tile_of(const DevGeom&, int ix, int iy, int tiles_x) {
+  return tile_of_pixel(ix, iy, tiles_x);
 }
 
-// A 4-bit step code holds (dx, dy) in {0,1} x {-1,0,1}. The reference's
-// tracer can emit a segment far from the previous one (float rounding with
-// the source a million units away, at near-vertical angles on the edge
-// columns): such a step starts a new run, as a tile change does.
-__device__ __forceinline__ bool unit_step(int ix, int iy, int px, int py) {
-  const int dx = ix - px, dy = iy - py;
-  return dx >= 0 && dx <= 1 && dy >= -1 && dy <= 1;
-}
+// ---- construction (runs per ray are counted by k_trace_count) ----------------
+// The segments of one ray, in order, as f(idx, length, 16-bit length code):
+// read back from the ray-ordered forward matrix when the plan keeps one
+// (delta-coded or explicit indices; the stored code is the one encode16 gives
+// the traced length, so both sources yield the same tile stream), traced
+// again otherwise (forward traced on the fly, or a stray step the 4-bit code
+// cannot hold).
+enum SegSource { kSrcTrace = 0, kSrcDelta = 1, kSrcIndex = 2 };
 
-// ---- construction --------------------------------------------------------------
-__global__ void __launch_bounds__(kTraceBlock)
-    k_runs_count(DevGeom G, int tiles_x, int* ray_nruns) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= (int64_t)G.P * G.C) return;
+template <int SRC, bool L16, class F>
+__device__ __forceinline__ void ray_segments(const DevGeom& G, const MatrixDev& M,
+                                             int64_t r, F&& f) {
   const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
-  int n = 0, cur = -1, px = 0, py = 0;
-  const int g = G.C;
-  trace_ray(G, a, c, [&](int idx, float, float) {
-    const int ix = idx % g, iy = idx / g;
-    const int t = tile_of(G, ix, iy, tiles_x);
-    if (t != cur || !unit_step(ix, iy, px, py)) {
-      ++n;
-      cur = t;
+  if constexpr (SRC == kSrcTrace) {
+    trace_ray(G, a, c, [&](int idx, float l, float) {
+      f(idx, l, L16 ? encode16(l, M.len_kind, M.scale) : (uint16_t)0);
+    });
+  } else {
+    const int g = G.C;
+    const int grp = a * G.gpa + (c >> 5), lane = c & 31;
+    const int n = M.rnseg[r];
+    const int64_t base = M.roff[grp] + lane;
+    const int64_t cbase = SRC == kSrcDelta ? M.rcoff[grp] + lane : 0;
+    int idx = (SRC == kSrcDelta && n > 0) ? M.rstart[r] : 0;
+    uint32_t word = 0;
+    for (int s = 0; s < n; ++s) {
+      const int64_t e = base + (int64_t)s * 32;
+      if constexpr (SRC == kSrcDelta) {
+        if ((s & 7) == 0) word = __ldcs(M.rcode + cbase + (int64_t)(s >> 3) * 32);
+        if (s > 0) {
+          const uint32_t code = (word >> (4 * (s & 7))) & 15u;
+          idx += (int)(code & 1u) + ((int)(code >> 1) - 1) * g;
+        }
+      } else {
+        idx = __ldcs(M.ridx + e);
+      }
+      if constexpr (L16)
+        f(idx, 0.f, __ldcs(reinterpret_cast<const uint16_t*>(M.rlen) + e));
+      else
+        f(idx, __ldcs(reinterpret_cast<const float*>(M.rlen) + e), (uint16_t)0);
     }
-    px = ix;
-    py = iy;
-  });
-  ray_nruns[r] = n;
+  }
 }
 
 // A run's sort key: (tile, chunk-count class, ray, ordinal). Within a tile
@@ -84,13 +97,13 @@ __device__ __forceinline__ unsigned long long run_key(RunKey rk, int t, int len,
          ((unsigned long long)r << 8) | (unsigned long long)(k & 255);
 }
 
+template <int SRC>
 __global__ void __launch_bounds__(kTraceBlock)
-    k_runs_emit(DevGeom G, int tiles_x, RunKey rk, const int64_t* ray_run_off,
-                unsigned long long* key, int* val, uint16_t* run_lp,
-                uint16_t* run_len, int* tile_count) {
+    k_runs_emit(DevGeom G, MatrixDev M, int tiles_x, RunKey rk,
+                const int64_t* ray_run_off, unsigned long long* key, int* val,
+                uint16_t* run_lp, uint16_t* run_len, int* tile_count) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= (int64_t)G.P * G.C) return;
-  const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
   const int g = G.C;
   int64_t i = ray_run_off[r] - 1;
   int cur = -1, k = -1, len = 0, px = 0, py = 0;
@@ -100,7 +113,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       key[i] = run_key(rk, cur, len, r, k);
     }
   };
-  trace_ray(G, a, c, [&](int idx, float, float) {
+  ray_segments<SRC, false>(G, M, r, [&](int idx, float, uint16_t) {
     const int ix = idx % g, iy = idx / g;
     const int t = tile_of(G, ix, iy, tiles_x);
     const bool step_ok = unit_step(ix, iy, px, py);
@@ -142,15 +155,13 @@ __global__ void k_runs_group(RunKey rk, const unsigned long long* skey, const in
   atomicMax(&gsteps[grp], (int)run_len[i]);
 }
 
-template <bool L16>
+template <bool L16, int SRC>
 __global__ void __launch_bounds__(kTraceBlock)
-    k_runs_fill(DevGeom G, int tiles_x, int len_kind, float scale,
-                const int64_t* ray_run_off, const int* run_slot,
-                const int64_t* gseg_off, const int64_t* gcode_off, void* tlen,
-                uint32_t* tcode) {
+    k_runs_fill(DevGeom G, MatrixDev M, int tiles_x, const int64_t* ray_run_off,
+                const int* run_slot, const int64_t* gseg_off,
+                const int64_t* gcode_off, void* tlen, uint32_t* tcode) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= (int64_t)G.P * G.C) return;
-  const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
   const int g = G.C;
   int64_t i = ray_run_off[r] - 1;
   int cur = -1, s = 0, px = 0, py = 0;
@@ -159,7 +170,7 @@ __global__ void __launch_bounds__(kTraceBlock)
   auto flush = [&]() {
     if (i >= ray_run_off[r] && (s & 7) != 0) tcode[cbase + (int64_t)(s >> 3) * 32] = word;
   };
-  trace_ray(G, a, c, [&](int idx, float l, float) {
+  ray_segments<SRC, L16>(G, M, r, [&](int idx, float l, uint16_t code) {
     const int ix = idx % g, iy = idx / g;
     const int t = tile_of(G, ix, iy, tiles_x);
     if (t != cur || !unit_step(ix, iy, px, py)) {
@@ -179,7 +190,7 @@ __global__ void __launch_bounds__(kTraceBlock)
     // entry (chunk s/8, lane, s%8): chunks of 8 steps, 32 lanes per chunk
     const int64_t e = lbase + (int64_t)(s >> 3) * 256 + (s & 7);
     if (L16)
-      reinterpret_cast<uint16_t*>(tlen)[e] = encode16(l, len_kind, scale);
+      reinterpret_cast<uint16_t*>(tlen)[e] = code;
     else
       reinterpret_cast<float*>(tlen)[e] = l;
     if ((s & 7) == 7) {
@@ -474,18 +485,30 @@ inline int blocks_for(int64_t n, int b) { return (int)((n + b - 1) / b); }
 
 }  // namespace
 
-void launch_runs_count(const DevGeom& G, int tiles_x, int* ray_nruns,
-                       cudaStream_t st) {
-  const int64_t R = (int64_t)G.P * G.C;
-  k_runs_count<<<blocks_for(R, kTraceBlock), kTraceBlock, 0, st>>>(G, tiles_x, ray_nruns);
+static int seg_source(const MatrixDev& M) {
+  if (M.rlen == nullptr) return kSrcTrace;
+  return M.rcode != nullptr ? kSrcDelta : kSrcIndex;
 }
 
-void launch_runs_emit(const DevGeom& G, int tiles_x, RunKey rk, const int64_t* ray_run_off,
-                      unsigned long long* key, int* val, uint16_t* run_lp,
-                      uint16_t* run_len, int* tile_count, cudaStream_t st) {
+void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, RunKey rk,
+                      const int64_t* ray_run_off, unsigned long long* key, int* val,
+                      uint16_t* run_lp, uint16_t* run_len, int* tile_count,
+                      cudaStream_t st) {
   const int64_t R = (int64_t)G.P * G.C;
-  k_runs_emit<<<blocks_for(R, kTraceBlock), kTraceBlock, 0, st>>>(
-      G, tiles_x, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+  const int blocks = blocks_for(R, kTraceBlock);
+  switch (seg_source(M)) {
+    case kSrcDelta:
+      k_runs_emit<kSrcDelta><<<blocks, kTraceBlock, 0, st>>>(
+          G, M, tiles_x, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+      break;
+    case kSrcIndex:
+      k_runs_emit<kSrcIndex><<<blocks, kTraceBlock, 0, st>>>(
+          G, M, tiles_x, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+      break;
+    default:
+      k_runs_emit<kSrcTrace><<<blocks, kTraceBlock, 0, st>>>(
+          G, M, tiles_x, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+  }
 }
 
 int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
@@ -515,19 +538,38 @@ void launch_runs_group(RunKey rk, const unsigned long long* skey, const int* sva
       glen, gsteps, run_slot);
 }
 
-void launch_runs_fill(const DevGeom& G, int tiles_x, int len_kind, float scale,
+template <bool L16>
+static void runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x,
+                      const int64_t* ray_run_off, const int* run_slot,
+                      const int64_t* gseg_off, const int64_t* gcode_off, void* tlen,
+                      uint32_t* tcode, cudaStream_t st) {
+  const int64_t R = (int64_t)G.P * G.C;
+  const int blocks = blocks_for(R, kTraceBlock);
+  switch (seg_source(M)) {
+    case kSrcDelta:
+      k_runs_fill<L16, kSrcDelta><<<blocks, kTraceBlock, 0, st>>>(
+          G, M, tiles_x, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
+      break;
+    case kSrcIndex:
+      k_runs_fill<L16, kSrcIndex><<<blocks, kTraceBlock, 0, st>>>(
+          G, M, tiles_x, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
+      break;
+    default:
+      k_runs_fill<L16, kSrcTrace><<<blocks, kTraceBlock, 0, st>>>(
+          G, M, tiles_x, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
+  }
+}
+
+void launch_runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x,
                       const int64_t* ray_run_off, const int* run_slot,
                       const int64_t* gseg_off, const int64_t* gcode_off,
                       void* tlen, uint32_t* tcode, cudaStream_t st) {
-  const int64_t R = (int64_t)G.P * G.C;
-  if (len_kind != LK_F32)
-    k_runs_fill<true><<<blocks_for(R, kTraceBlock), kTraceBlock, 0, st>>>(
-        G, tiles_x, len_kind, scale, ray_run_off, run_slot, gseg_off, gcode_off,
-        tlen, tcode);
+  if (M.len_kind != LK_F32)
+    runs_fill<true>(G, M, tiles_x, ray_run_off, run_slot, gseg_off, gcode_off, tlen,
+                    tcode, st);
   else
-    k_runs_fill<false><<<blocks_for(R, kTraceBlock), kTraceBlock, 0, st>>>(
-        G, tiles_x, len_kind, scale, ray_run_off, run_slot, gseg_off, gcode_off,
-        tlen, tcode);
+    runs_fill<false>(G, M, tiles_x, ray_run_off, run_slot, gseg_off, gcode_off, tlen,
+                     tcode, st);
 }
 
 void launch_forward_tiled(const IterArgs& A, const TileMatrixDev& T,

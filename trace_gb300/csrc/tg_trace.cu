@@ -17,7 +17,7 @@ constexpr int kTraceBlock = 128;
 
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_count(DevGeom G, int ngroups, int* nseg, int* rcap,
-                  unsigned* maxlen_bits) {
+                  unsigned* maxlen_bits, int tiles_x, int* ray_nruns) {
   const int grp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (grp >= ngroups) return;  // warp-uniform
@@ -26,7 +26,24 @@ __global__ void __launch_bounds__(kTraceBlock)
   int n = 0;
   float ml = 0.f;
   if (c < G.C) {
-    n = trace_ray(G, a, c, [&](int, float l, float) { ml = fmaxf(ml, l); });
+    if (ray_nruns) {
+      const int g = G.C;
+      int runs = 0, cur = -1, px = 0, py = 0;
+      n = trace_ray(G, a, c, [&](int idx, float l, float) {
+        ml = fmaxf(ml, l);
+        const int ix = idx % g, iy = idx / g;
+        const int t = tile_of_pixel(ix, iy, tiles_x);
+        if (t != cur || !unit_step(ix, iy, px, py)) {
+          ++runs;
+          cur = t;
+        }
+        px = ix;
+        py = iy;
+      });
+      ray_nruns[(int64_t)a * G.C + c] = runs;
+    } else {
+      n = trace_ray(G, a, c, [&](int, float l, float) { ml = fmaxf(ml, l); });
+    }
     nseg[(int64_t)a * G.C + c] = n;
   }
   const int cap = warp_max_i(n);
@@ -209,11 +226,12 @@ __global__ void __launch_bounds__(kTraceBlock)
 }  // namespace
 
 void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
-                        unsigned* maxlen_bits, cudaStream_t st) {
+                        unsigned* maxlen_bits, int tiles_x, int* ray_nruns,
+                        cudaStream_t st) {
   const int ngroups = G.P * G.gpa;
   const int blocks = (ngroups * 32 + kTraceBlock - 1) / kTraceBlock;
   k_trace_count<<<blocks, kTraceBlock, 0, st>>>(G, ngroups, nseg, rcap,
-                                                 maxlen_bits);
+                                                 maxlen_bits, tiles_x, ray_nruns);
 }
 
 void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
