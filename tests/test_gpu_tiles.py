@@ -90,7 +90,9 @@ def test_half_gathers_against_fp64(alg, K, S):
 
 def test_half_gathers_keep_operator_path_fp32():
     """tg_reduce (the reference's RunParallelReduction) runs the ray-ordered
-    forward with FP32 factors on a half_gathers plan: identical replica."""
+    forward with FP32 factors on a half_gathers plan; its backward matrix
+    holds the lengths as halves, so the replica agrees with the plain plan's
+    to the rounding of the lengths (relative L2 <= 1e-4)."""
     C, P, S = 64, 40, 4
     th = theta_uniform(P)
     rng = np.random.default_rng(7)
@@ -105,7 +107,7 @@ def test_half_gathers_keep_operator_path_fp32():
         plan.reduce("pml", prm)
         reps.append(plan.get_replica("pml"))
         plan.close()
-    assert np.array_equal(bits(reps[0]), bits(reps[1]))
+    assert rel_l2(reps[1], reps[0]) < 1e-4
 
 
 @pytest.mark.parametrize("kw", [dict(mode="fast"), dict(mode="exact", forward_tiles=True),

@@ -211,16 +211,22 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
       if constexpr (FH && !EXACT && K >= 2 && K <= 8) {
         // software pipeline over the quad's 4 angles: the factor loads of
         // angle j + 1 are in flight while angle j's FMAs run
-        uint32_t w0[2][K / 2], w1[2][K / 2];
-        unsigned short lh0[2], lh1[2];
+        // lw[b]: the two half lengths of the angle (slot 0 low, slot 1 high)
+        uint32_t w0[2][K / 2], w1[2][K / 2], lw[2];
         auto issue = [&](int j, int b) {
-          float l0, l1;
           bool h0, h1;
-          quad_pair<LK, false>(q, j, A.M.inv_scale, l0, l1, h0, h1);
+          if constexpr (LK == LK_F16) {
+            // stored as halves: the FMA operands as they are
+            lw[b] = pick(q.w[0], j);
+            h0 = (lw[b] & 0xffffu) != 0u;
+            h1 = (lw[b] >> 16) != 0u;
+          } else {
+            float l0, l1;
+            quad_pair<LK, false>(q, j, A.M.inv_scale, l0, l1, h0, h1);
+            lw[b] = float2_to_half2_bits(l0, l1);
+          }
           const int c0 = window_c0(s_coef[a4 + j], xf, yf);
           const __half* hb = reinterpret_cast<const __half*>(ua) + j * ck + c0 * K;
-          lh0[b] = __half_as_ushort(__float2half_rn(l0));
-          lh1[b] = __half_as_ushort(__float2half_rn(l1));
 #pragma unroll
           for (int i = 0; i < K / 2; ++i) { w0[b][i] = 0u; w1[b][i] = 0u; }
           if (h0) load_hwords<K>(w0[b], hb);
@@ -229,12 +235,12 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
         auto consume = [&](int b) {
 #pragma unroll
           for (int i = 0; i < K / 2; ++i) {
-            asm("{ .reg .b16 lo, hi; mov.b32 {lo, hi}, %2; fma.rn.f32.f16 %0, lo, %3, %0;"
-                " fma.rn.f32.f16 %1, hi, %3, %1; }"
-                : "+f"(acc[2 * i]), "+f"(acc[2 * i + 1]) : "r"(w0[b][i]), "h"(lh0[b]));
-            asm("{ .reg .b16 lo, hi; mov.b32 {lo, hi}, %2; fma.rn.f32.f16 %0, lo, %3, %0;"
-                " fma.rn.f32.f16 %1, hi, %3, %1; }"
-                : "+f"(acc[2 * i]), "+f"(acc[2 * i + 1]) : "r"(w1[b][i]), "h"(lh1[b]));
+            asm("{ .reg .b16 lo, hi, l0, l1; mov.b32 {lo, hi}, %2; mov.b32 {l0, l1}, %3;"
+                " fma.rn.f32.f16 %0, lo, l0, %0; fma.rn.f32.f16 %1, hi, l0, %1; }"
+                : "+f"(acc[2 * i]), "+f"(acc[2 * i + 1]) : "r"(w0[b][i]), "r"(lw[b]));
+            asm("{ .reg .b16 lo, hi, l0, l1; mov.b32 {lo, hi}, %2; mov.b32 {l0, l1}, %3;"
+                " fma.rn.f32.f16 %0, lo, l1, %0; fma.rn.f32.f16 %1, hi, l1, %1; }"
+                : "+f"(acc[2 * i]), "+f"(acc[2 * i + 1]) : "r"(w1[b][i]), "r"(lw[b]));
           }
         };
         issue(0, 0);
@@ -343,7 +349,7 @@ void back_launch(const IterArgs& A, int batch, const float* cur, float* next,
 template <int K>
 void back_kind(const IterArgs& A, int batch, const float* cur, float* next,
                const float* upd, float* rep_num, int epi, cudaStream_t st) {
-  switch (A.M.len_kind) {
+  switch (A.M.dlen_kind) {
     case LK_F32: back_launch<K, LK_F32>(A, batch, cur, next, upd, rep_num, epi, st); break;
     case LK_BF16: back_launch<K, LK_BF16>(A, batch, cur, next, upd, rep_num, epi, st); break;
     case LK_F16: back_launch<K, LK_F16>(A, batch, cur, next, upd, rep_num, epi, st); break;

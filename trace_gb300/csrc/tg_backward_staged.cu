@@ -292,7 +292,7 @@ void staged_launch(const IterArgs& A, int batch, const float* cur, float* next,
 template <int K>
 void staged_kind(const IterArgs& A, int batch, const float* cur, float* next,
                  const float* upd, float* rep_num, int epi, cudaStream_t st) {
-  switch (A.M.len_kind) {
+  switch (A.M.dlen_kind) {
     case LK_F32: staged_launch<K, LK_F32>(A, batch, cur, next, upd, rep_num, epi, st); break;
     case LK_BF16: staged_launch<K, LK_BF16>(A, batch, cur, next, upd, rep_num, epi, st); break;
     case LK_F16: staged_launch<K, LK_F16>(A, batch, cur, next, upd, rep_num, epi, st); break;

@@ -37,7 +37,10 @@ struct MatrixDev {
   int P4;              // angles rounded up to a multiple of 4 (padding empty)
   const float* W;      // [g*g] total length through each pixel
   const float* Wh;     // [g*g] the same over half-rounded lengths (half_gathers)
-  int len_kind;        // LenKind
+  int len_kind;        // LenKind of the forward matrices
+  // LenKind of the backward matrix: IEEE halves with half gathers (the
+  // backprojection's mixed-precision FMAs take them as stored), else len_kind
+  int dlen_kind;
   float scale, inv_scale;
 };
 

@@ -670,6 +670,9 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   M.W = p->d_W;
   M.Wh = p->d_Wh;
   M.len_kind = p->len_kind;
+  // half gathers: the backward matrix holds IEEE halves (same size as the
+  // 16-bit codes), the operands of the backprojection's mixed FMAs
+  M.dlen_kind = (d.half_gathers && l16) ? (int)LK_F16 : p->len_kind;
   M.scale = maxlen > 0 ? 65535.f / maxlen : 1.f;
   M.inv_scale = maxlen > 0 ? maxlen / 65535.f : 1.f;
 

@@ -127,9 +127,9 @@ __global__ void __launch_bounds__(kTraceBlock)
       const int64_t pos = dense_pair(M.ntiles, a, tile, tl) * 2 + slot;
       if (L16) {
         uint16_t* d = reinterpret_cast<uint16_t*>(dlen);
-        const float cur = decode16(d[pos], M.len_kind, M.inv_scale);
-        uint16_t code = encode16(cur + l, M.len_kind, M.scale);
-        if (code == 0 && M.len_kind != LK_U16) code = 0x8000u;
+        const float cur = decode16(d[pos], M.dlen_kind, M.inv_scale);
+        uint16_t code = encode16(cur + l, M.dlen_kind, M.scale);
+        if (code == 0 && M.dlen_kind != LK_U16) code = 0x8000u;
         d[pos] = code;
       } else {
         float* d = reinterpret_cast<float*>(dlen);
@@ -172,8 +172,8 @@ __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W) {
     if (L16) {
       const uint32_t w =
           reinterpret_cast<const uint32_t*>(M.dlen)[pos >> 1];
-      l0 = decode16((uint16_t)(w & 0xffffu), M.len_kind, M.inv_scale);
-      l1 = decode16((uint16_t)(w >> 16), M.len_kind, M.inv_scale);
+      l0 = decode16((uint16_t)(w & 0xffffu), M.dlen_kind, M.inv_scale);
+      l1 = decode16((uint16_t)(w >> 16), M.dlen_kind, M.inv_scale);
     } else {
       const float2 v = reinterpret_cast<const float2*>(M.dlen)[pos >> 1];
       l0 = v.x;
