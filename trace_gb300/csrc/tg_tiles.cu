@@ -167,8 +167,39 @@ __global__ void __launch_bounds__(kTraceBlock)
   int cur = -1, s = 0, px = 0, py = 0;
   int64_t lbase = 0, cbase = 0;
   uint32_t word = kStayWord;
-  auto flush = [&]() {
-    if (i >= ray_run_off[r] && (s & 7) != 0) tcode[cbase + (int64_t)(s >> 3) * 32] = word;
+  // the current chunk's 8 lengths as a shift register (oldest in the low
+  // bits), stored whole: one 16-byte write per chunk and lane (32 for f32)
+  uint32_t q[L16 ? 4 : 8] = {};
+  auto push = [&](uint32_t v) {
+    if constexpr (L16) {
+      q[0] = __funnelshift_r(q[0], q[1], 16);
+      q[1] = __funnelshift_r(q[1], q[2], 16);
+      q[2] = __funnelshift_r(q[2], q[3], 16);
+      q[3] = (q[3] >> 16) | (v << 16);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 7; ++k) q[k] = q[k + 1];
+      q[7] = v;
+    }
+  };
+  // entries (chunk c, lane, 0..7): chunks of 8 steps, 32 lanes per chunk
+  auto store = [&](int c) {
+    const int64_t e = lbase + (int64_t)c * 256;
+    if constexpr (L16) {
+      *reinterpret_cast<uint4*>(reinterpret_cast<uint16_t*>(tlen) + e) =
+          make_uint4(q[0], q[1], q[2], q[3]);
+    } else {
+      uint4* d = reinterpret_cast<uint4*>(reinterpret_cast<float*>(tlen) + e);
+      d[0] = make_uint4(q[0], q[1], q[2], q[3]);
+      d[1] = make_uint4(q[4], q[5], q[6], q[7]);
+    }
+    tcode[cbase + (int64_t)c * 32] = word;
+  };
+  auto flush = [&]() {  // a run's last, partial chunk: zero lengths after it
+    if (i >= ray_run_off[r] && (s & 7) != 0) {
+      for (int k = s & 7; k < 8; ++k) push(0u);
+      store(s >> 3);
+    }
   };
   ray_segments<SRC, L16>(G, M, r, [&](int idx, float l, uint16_t code) {
     const int ix = idx % g, iy = idx / g;
@@ -187,14 +218,9 @@ __global__ void __launch_bounds__(kTraceBlock)
       const int sh = 4 * (s & 7);
       word = (word & ~(15u << sh)) | ((uint32_t)((ix - px) | ((iy - py + 1) << 1)) << sh);
     }
-    // entry (chunk s/8, lane, s%8): chunks of 8 steps, 32 lanes per chunk
-    const int64_t e = lbase + (int64_t)(s >> 3) * 256 + (s & 7);
-    if (L16)
-      reinterpret_cast<uint16_t*>(tlen)[e] = code;
-    else
-      reinterpret_cast<float*>(tlen)[e] = l;
+    push(L16 ? (uint32_t)code : __float_as_uint(l));
     if ((s & 7) == 7) {
-      tcode[cbase + (int64_t)(s >> 3) * 32] = word;
+      store(s >> 3);
       word = kStayWord;
     }
     px = ix;
@@ -383,7 +409,6 @@ __global__ void __launch_bounds__(kBlock)
     if (chunks > 0) load_chunk<LK>(T, lb, cb, 0, cur);
     for (int c = 0; c < chunks; ++c) {
       if (c + 1 < chunks) load_chunk<LK>(T, lb, cb, c + 1, nxt);
-      const int s0 = c * 8;
       // No per-step guard: a run's first step and every step past its end
       // carry the "stay" code and a zero length (see k_runs_fill), so
       // lanes of shorter runs add 0 * (a finite pixel value) in place.
