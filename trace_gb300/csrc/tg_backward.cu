@@ -14,7 +14,9 @@
 // With half factors (fast mode, ratio algorithms) each factor is read as the
 // half (factor - 1) - half the gather bytes - and sum(len * factor) is
 // rebuilt as W + sum(len * (factor - 1)), the products taken by
-// mixed-precision FMAs straight from the halves.
+// mixed-precision FMAs straight from the halves; the plan then stores the
+// backward matrix's lengths as halves too (MatrixDev::dlen_kind), so both
+// FMA operands come from memory as they are.
 //
 // Epilogue per slice: SIRT recon += num/W (sirt.cc:21-33), MLEM
 // recon *= num/W (mlem.cc:21-34), PML/APMLR the closed-form root with the
