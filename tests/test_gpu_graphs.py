@@ -58,3 +58,26 @@ def test_batch_matches_individual_plans():
     batch.close()
     for p in plans:
         p.close()
+
+
+def test_plans_created_from_host_threads():
+    """Plans created and iterated concurrently from several host threads
+    (each plan traces on its own stream) give the same results as plans
+    created one after another (exact mode: bit-identical)."""
+    from concurrent.futures import ThreadPoolExecutor
+    cases = [(64, 48, 3, 11, "sirt"), (96, 40, 2, 12, "mlem"), (80, 60, 4, 13, "pml"),
+             (48, 36, 5, 14, "apmlr"), (72, 30, 1, 15, "sirt"), (56, 64, 3, 16, "mlem")]
+
+    def run(case):
+        C, P, S, seed, alg = case
+        plan = _plan(C, P, S, seed, alg, slices_per_pass=1)
+        plan.iterate(alg, 2, tg.default_params(alg, beta=0.3))
+        out = plan.get_recon(alg)
+        plan.close()
+        return out
+
+    serial = [run(c) for c in cases]
+    with ThreadPoolExecutor(4) as ex:
+        threaded = list(ex.map(run, cases))
+    for a, b in zip(serial, threaded):
+        assert np.array_equal(bits(a), bits(b))
