@@ -89,10 +89,10 @@ def test_half_gathers_against_fp64(alg, K, S):
 
 
 def test_half_gathers_keep_operator_path_fp32():
-    """tg_reduce (the reference's RunParallelReduction) runs the ray-ordered
-    forward with FP32 factors on a half_gathers plan; its backward matrix
-    holds the lengths as halves, so the replica agrees with the plain plan's
-    to the rounding of the lengths (relative L2 <= 1e-4)."""
+    """tg_reduce (the reference's RunParallelReduction) runs the tile-ordered
+    forward with FP32 factors on a half_gathers plan (half tile, f16 lengths
+    in the backward matrix), so its replica agrees with the plain tiled
+    plan's to the rounding of those operands (relative L2 <= 1e-4)."""
     C, P, S = 64, 40, 4
     th = theta_uniform(P)
     rng = np.random.default_rng(7)
@@ -144,3 +144,55 @@ def test_sixteen_slices_with_tiles_need_half_gathers():
         tg.Plan(8, 16, 16, theta_uniform(8), slices_per_pass=16, mode="fast",
                 forward_tiles=True)
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16", "bf16", "u16"])
+def test_half_gathers_with_each_length_storage(storage):
+    """Half gathers over every forward length storage: 16-bit storages keep
+    f16 lengths in the backward matrix (the FMA operands as stored), f32
+    storage keeps f32 lengths there and rounds them per FMA."""
+    C, P, S, it = 80, 60, 8, 5
+    th = theta_uniform(P)
+    tabs = O.angle_table(th)
+    from trace_gb300.phantom import ellipse_phantoms
+    sino = O.forward(ellipse_phantoms(C, S, seed=9, texture_sigma=0.02), tabs)
+    ref = O.run("mlem", sino, tables=tabs, n_iter=it, precision=O.F64)["recon"]
+    plan = tg.Plan(P, S, C, th, slices_per_pass=8, mode="fast", len_storage=storage,
+                   delta_index=True, forward_tiles=True, half_gathers=True)
+    plan.set_sinogram(sino, apply_abs=True)
+    plan.reset_recon("mlem")
+    plan.iterate("mlem", it, tg.default_params("mlem"))
+    err = rel_l2(plan.get_recon("mlem"), ref)
+    plan.close()
+    assert err < (3e-3 if storage == "bf16" else 2e-4), err
+
+
+@pytest.mark.parametrize("alg", ["sirt", "mlem", "pml", "apmlr"])
+def test_operator_path_uses_tiles(alg):
+    """reduce -> replica and forward_project on a tile-ordered plan agree with
+    the ray-ordered plan of the same storage (sums by atomics: relative
+    L2 <= 1e-6), as the drivers' RunParallelReduction / UpdateRecon loop
+    calls them."""
+    C, P, S = 72, 54, 6
+    th = theta_uniform(P)
+    rng = np.random.default_rng(17)
+    sino = rng.uniform(0.5, 2.0, (P, S, C)).astype(np.float32)
+    prm = tg.default_params(alg, beta=0.1)
+    reps, sims, recons = [], [], []
+    for tiles in (False, True):
+        plan = tg.Plan(P, S, C, th, slices_per_pass=2, mode="fast", len_storage="u16",
+                       delta_index=True, forward_tiles=tiles)
+        plan.set_sinogram(sino, apply_abs=alg != "sirt")
+        plan.reset_recon(alg)
+        for _ in range(2):  # reference driver loop: Reduce, then UpdateRecon
+            plan.reduce(alg, prm)
+            if alg in ("pml", "apmlr"):
+                plan.calculate_fg(alg, prm)
+            plan.update_recon(alg, prm)
+        reps.append(plan.get_replica(alg))
+        recons.append(plan.get_recon(alg))
+        sims.append(plan.forward_project(alg))
+        plan.close()
+    assert rel_l2(reps[1], reps[0]) < 1e-6
+    assert rel_l2(recons[1], recons[0]) < 1e-6
+    assert rel_l2(sims[1], sims[0]) < 1e-6

@@ -950,9 +950,26 @@ int tg_get_recon(tg_plan* p, int alg, float* recon, int on_device) {
   return TG_OK;
 }
 
-static int run_forward(tg_plan* p, const IterArgs& A, int b, int out_mode,
+// Forward projection of batch b into per-ray values `out` (FP32): the
+// tile-ordered kernel (ray sums by atomics, plus the finish kernel) when the
+// plan has the tile-ordered matrix, else the ray-ordered kernel.
+static int run_forward(tg_plan* p, const IterArgs& A0, int b, int out_mode,
                        float* out) {
   const float* src = batch_ptr(p, p->d_recon[p->cur], b * p->K + p->fshift);
+  if (p->tiles) {
+    IterArgs A = A0;
+    A.half_tile = p->d.half_gathers;
+    A.half_factors = 0;
+    {
+      Timed t(p, 0);
+      launch_forward_tiled(A, p->T, src, p->d_sim, p->st);
+    }
+    Timed t(p, 2);
+    launch_fwd_finish(A, p->d_sim, p->d_sino ? p->d_sino + (int64_t)b * p->R * p->K : nullptr,
+                      out, out_mode, p->st);
+    return TG_OK;
+  }
+  const IterArgs& A = A0;
   Timed t(p, 0);
   launch_forward(A, src, p->d_sino + (int64_t)b * p->R * p->K, out, out_mode,
                  p->st);
