@@ -247,3 +247,31 @@ def test_get_recon_into_host_buffers():
     with pytest.raises(ValueError):
         plan.get_recon(alg, out=np.empty(want.shape, np.float64))
     plan.close()
+
+
+@pytest.mark.parametrize("P", [1920, 1921, 2003])
+def test_many_angles(P):
+    """Angle counts past several 512-angle chunks of the backprojection's
+    staged window coefficients (and not a multiple of 4): against the oracle
+    (exact mode) and FP64 (fast mode with half gathers)."""
+    C, S, it = 32, 2, 2
+    th = theta_uniform(P)
+    tabs = O.angle_table(th)
+    rng = np.random.default_rng(P)
+    sino = rng.uniform(0.5, 2.0, (P, S, C)).astype(np.float32)
+    want = O.run("mlem", sino, tables=tabs, n_iter=it)["recon"]
+    plan = tg.Plan(P, S, C, th, sin_tab=tabs[0], cos_tab=tabs[1])
+    plan.set_sinogram(sino, apply_abs=True)
+    plan.reset_recon("mlem")
+    plan.iterate("mlem", it)
+    assert rel_l2(plan.get_recon("mlem"), want) < 2e-6
+    plan.close()
+    ref = O.run("mlem", sino, tables=tabs, n_iter=it, precision=O.F64)["recon"]
+    plan = tg.Plan(P, S, C, th, sin_tab=tabs[0], cos_tab=tabs[1], slices_per_pass=2,
+                   mode="fast", len_storage="u16", delta_index=True, forward_tiles=True,
+                   half_gathers=True)
+    plan.set_sinogram(sino, apply_abs=True)
+    plan.reset_recon("mlem")
+    plan.iterate("mlem", it)
+    assert rel_l2(plan.get_recon("mlem"), ref) < 2e-4
+    plan.close()

@@ -154,6 +154,17 @@ void launch_forward(const IterArgs& A, const float* recon_batch,
                     const float* sino_batch, float* out, int out_mode,
                     cudaStream_t st);
 // tg_backward.cu
+// per-K instances of launch_backward (tg_backward*.cu)
+#define TG_BACKWARD_DECL(KK)                                                      \
+  void launch_backward_k##KK(const IterArgs& A, int batch, const float* recon_cur, \
+                             float* recon_next, const float* upd, float* rep_num, \
+                             int epi, cudaStream_t st);
+TG_BACKWARD_DECL(1)
+TG_BACKWARD_DECL(2)
+TG_BACKWARD_DECL(4)
+TG_BACKWARD_DECL(8)
+TG_BACKWARD_DECL(16)
+#undef TG_BACKWARD_DECL
 void launch_backward(const IterArgs& A, int batch, const float* recon_cur,
                      float* recon_next, const float* upd, float* rep_num,
                      int epi, cudaStream_t st);
