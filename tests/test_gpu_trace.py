@@ -71,3 +71,28 @@ def test_matrix_storage_variants_build(storage, delta):
     assert info["num_segments"] > 0
     assert 1.41 < info["max_segment_length"] < 1.6
     plan.close()
+
+
+@pytest.mark.parametrize("C", [64, 37])
+def test_gpu_trace_degenerate_angles(C):
+    """The tracer's bisection for the first crossing inside the grid and its
+    stop at the first one outside give the reference's trimmed lists also
+    where the slopes are zero, infinite or tiny: exact 0 / 90 degree tables,
+    subnormal and tiny angles, one ulp around 90 degrees, negative and
+    beyond-2pi angles."""
+    half_pi = np.float32(np.pi / 2)
+    th = np.array([0.0, 1e-30, 1e-39, 1e-7, half_pi,
+                   np.nextafter(half_pi, np.float32(2)), np.nextafter(half_pi, np.float32(0)),
+                   np.pi, 3 * np.pi / 2, -0.3, 7.0, 2.5], np.float32)
+    s, c, q = O.angle_table(th)
+    s, c = s.copy(), c.copy()
+    s[4], c[4] = 1.0, 0.0      # exact tables at 90 degrees
+    s[7], c[7] = 0.0, -1.0     # and at 180 degrees
+    plan = tg.Plan(th.size, 1, C, th, sin_tab=s, cos_tab=c)
+    g = plan.trace_rays()
+    o = O.trace(C, (s, c, q))
+    assert np.array_equal(g[0], o[0])
+    assert np.array_equal(g[2], o[2])
+    assert np.array_equal(bits(g[3]), bits(o[3]))
+    assert np.array_equal(bits(g[4]), bits(o[4]))
+    plan.close()

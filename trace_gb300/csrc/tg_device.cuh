@@ -44,9 +44,30 @@ __device__ __forceinline__ float grid_line(const DevGeom& G, int n) {
 // Returns the number of segments emitted.
 //
 // Crossings with horizontal grid lines ("a" points) and vertical grid lines
-// ("b" points) are walked by two cursors that skip crossings outside the
-// open grid square; the a cursor runs backwards for quadrant-0 angles (the
+// ("b" points) are walked by two cursors over the crossings inside the open
+// grid square; the a cursor runs backwards for quadrant-0 angles (the
 // reversed a list of SortIntersectionPoints) and ties go to b.
+//
+// Each list's coordinate is a monotone function of the line index (rounded
+// subtraction, multiplication by a constant and addition are monotone), so
+// the crossings strictly inside the square are one contiguous run of line
+// indices. The first one is found by bisection, and a cursor stops at the
+// first crossing outside: the same points the reference's trim keeps,
+// without evaluating the lines outside the square.
+
+// First k in [0, n] with pred(k) for a predicate that is false up to some k
+// and true from there on; n + 1 if none.
+template <class Pred>
+__device__ __forceinline__ int first_true(int n, Pred&& pred) {
+  int lo = 0, hi = n + 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (pred(mid)) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
 template <class Emit>
 __device__ __forceinline__ int trace_ray(const DevGeom& G, int a, int c,
                                          Emit&& emit) {
@@ -62,18 +83,36 @@ __device__ __forceinline__ int trace_ray(const DevGeom& G, int a, int c,
   const float islope = fdiv(1.0f, slope);
   const float lo = grid_line(G, 0), hi = grid_line(G, g);
 
+  auto eval_a = [&](int n) { return fadd(fmul(islope, fsub(grid_line(G, n), srcy)), srcx); };
+  auto eval_b = [&](int n) { return fadd(fmul(slope, fsub(grid_line(G, n), srcx)), srcy); };
+  auto inside = [&](float v) { return v > lo && v < hi; };
+
+  // a list: line na0 + k*da for k = 0..g, coordinate non-decreasing in k
+  // when islope*da >= 0 (NaN and infinities at 0 and 90 degrees keep the
+  // predicates below monotone; no such point is inside)
   const int da = G.quad[a] ? 1 : -1;
-  int na = G.quad[a] ? 0 : g;
+  const int na0 = G.quad[a] ? 0 : g;
+  const bool a_up = da > 0 ? !signbit(islope) : signbit(islope);
+  const int ka = first_true(g, [&](int k) {
+    const float v = eval_a(na0 + k * da);
+    return a_up ? v > lo : v < hi;
+  });
+  int na = na0 + ka * da;  // out of [0, g] when the list is exhausted
   float ax = 0.f;
-  for (; na >= 0 && na <= g; na += da) {
-    ax = fadd(fmul(islope, fsub(grid_line(G, na), srcy)), srcx);
-    if (ax > lo && ax < hi) break;
+  if (ka <= g) {
+    ax = eval_a(na);
+    if (!inside(ax)) na = -1;
   }
-  int nb = 0;
+  // b list: line nb for nb = 0..g, non-decreasing when slope >= 0
+  const bool b_up = !signbit(slope);
+  int nb = first_true(g, [&](int k) {
+    const float v = eval_b(k);
+    return b_up ? v > lo : v < hi;
+  });
   float by = 0.f;
-  for (; nb <= g; ++nb) {
-    by = fadd(fmul(slope, fsub(grid_line(G, nb), srcx)), srcy);
-    if (by > lo && by < hi) break;
+  if (nb <= g) {
+    by = eval_b(nb);
+    if (!inside(by)) nb = g + 1;
   }
 
   int nseg = 0;
@@ -87,16 +126,18 @@ __device__ __forceinline__ int trace_ray(const DevGeom& G, int a, int c,
     if (take_a) {
       x = ax;
       y = grid_line(G, na);
-      for (na += da; na >= 0 && na <= g; na += da) {
-        ax = fadd(fmul(islope, fsub(grid_line(G, na), srcy)), srcx);
-        if (ax > lo && ax < hi) break;
+      na += da;
+      if (na >= 0 && na <= g) {
+        ax = eval_a(na);
+        if (!inside(ax)) na = -1;  // the run of inside crossings ended
       }
     } else {
       x = grid_line(G, nb);
       y = by;
-      for (++nb; nb <= g; ++nb) {
-        by = fadd(fmul(slope, fsub(grid_line(G, nb), srcx)), srcy);
-        if (by > lo && by < hi) break;
+      ++nb;
+      if (nb <= g) {
+        by = eval_b(nb);
+        if (!inside(by)) nb = g + 1;
       }
     }
     if (have_prev) {
