@@ -39,7 +39,8 @@ __device__ __forceinline__ float grid_line(const DevGeom& G, int n) {
   return fsub((float)n, G.halfg);
 }
 
-// Streams the segments of ray (a, c) to emit(idx, len, len2) in the order of
+// Streams the segments of ray (a, c) to emit(idx, len, len2, ix, iy) (ix,
+// iy: column and row of cell idx = iy * g + ix) in the order of
 // the reference tracer (trace_utils.cc:48-216 composed as sirt.cc:126-160).
 // Returns the number of segments emitted.
 //
@@ -153,7 +154,10 @@ __device__ __forceinline__ int trace_ray(const DevGeom& G, int a, int c,
       // A stray segment whose cell index falls outside the grid (the
       // reference indexes its arrays out of bounds there) is dropped.
       if ((unsigned)idx < (unsigned)g * (unsigned)g) {
-        emit(idx, len, len2);
+        // the cell idx names (a stray segment's column can lie outside the
+        // grid while its index is inside: then idx, not ix, decides)
+        if ((unsigned)ix < (unsigned)g) emit(idx, len, len2, ix, iy);
+        else emit(idx, len, len2, idx % g, idx / g);
         ++nseg;
       }
     }
@@ -162,6 +166,24 @@ __device__ __forceinline__ int trace_ray(const DevGeom& G, int a, int c,
     have_prev = true;
   }
   return nseg;
+}
+
+// Column and row of cell idx in [0, g*g), g < 2^23, without an integer
+// division: the float quotient estimate is off by at most one (its relative
+// error is a few 2^-24, i.e. below 1/g in absolute terms) and is corrected
+// exactly from the remainder.
+__device__ __forceinline__ void cell_xy(int idx, int g, float inv_g, int& ix, int& iy) {
+  int q = __float2int_rz(__fmul_rn(__int2float_rn(idx), inv_g));
+  int rem = idx - q * g;
+  if (rem < 0) {
+    --q;
+    rem += g;
+  } else if (rem >= g) {
+    ++q;
+    rem -= g;
+  }
+  ix = rem;
+  iy = q;
 }
 
 // First detector column of the two-column window that holds every ray

@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(kBlock)
   float acc[K];
 #pragma unroll
   for (int j = 0; j < K; ++j) acc[j] = 0.f;
-  trace_ray(G, a, c, [&](int idx, float l, float) {
+  trace_ray(G, a, c, [&](int idx, float l, float, int, int) {
     const Vec<K> v = load_vec<K>(recon + (int64_t)idx * K);
     if constexpr (EXACT) {
 #pragma unroll

@@ -144,8 +144,9 @@ __device__ __forceinline__ void for_each_exception(const MatrixDev& M, int tile,
     if (x.x == lane) f(__int_as_float(x.w), x.y, x.z);
   }
 }
+// W (and, when Wh is given, the total of the half-rounded lengths) per pixel
 void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
-                    cudaStream_t st, bool half_lengths = false);
+                    float* Wh, cudaStream_t st);
 void launch_trace_export(const DevGeom& G, const int64_t* offsets, int* idx,
                          float* len, float* len2, cudaStream_t st);
 

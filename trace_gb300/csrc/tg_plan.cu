@@ -748,8 +748,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     M.rlen = nullptr;
     p->info.forward_traced = 1;
   }
-  launch_weights(G, M, d.mode == TG_MODE_EXACT, p->d_W, p->st);
-  if (p->d_Wh) launch_weights(G, M, 0, p->d_Wh, p->st, true);
+  launch_weights(G, M, d.mode == TG_MODE_EXACT, p->d_W, p->d_Wh, p->st);
   if (p->fp64) launch_weights64(G, M, p->d_W64, p->st);
   p->info.window_exceptions = (int64_t)nexc;
   (void)counters[1];

@@ -42,7 +42,8 @@ __device__ __forceinline__ int tile_of(const DevGeom&, int ix, int iy, int tiles
 }
 
 // ---- construction (runs per ray are counted by k_trace_count) ----------------
-// The segments of one ray, in order, as f(idx, length, 16-bit length code):
+// The segments of one ray, in order, as f(idx, ix, iy, length, 16-bit length
+// code), idx = iy * g + ix:
 // read back from the ray-ordered forward matrix when the plan keeps one
 // (delta-coded or explicit indices; the stored code is the one encode16 gives
 // the traced length, so both sources yield the same tile stream), traced
@@ -55,8 +56,8 @@ __device__ __forceinline__ void ray_segments(const DevGeom& G, const MatrixDev& 
                                              int64_t r, F&& f) {
   const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
   if constexpr (SRC == kSrcTrace) {
-    trace_ray(G, a, c, [&](int idx, float l, float) {
-      f(idx, l, L16 ? encode16(l, M.len_kind, M.scale) : (uint16_t)0);
+    trace_ray(G, a, c, [&](int idx, float l, float, int ix, int iy) {
+      f(idx, ix, iy, l, L16 ? encode16(l, M.len_kind, M.scale) : (uint16_t)0);
     });
   } else {
     const int g = G.C;
@@ -64,7 +65,10 @@ __device__ __forceinline__ void ray_segments(const DevGeom& G, const MatrixDev& 
     const int n = M.rnseg[r];
     const int64_t base = M.roff[grp] + lane;
     const int64_t cbase = SRC == kSrcDelta ? M.rcoff[grp] + lane : 0;
+    const float inv_g = 1.0f / (float)g;
     int idx = (SRC == kSrcDelta && n > 0) ? M.rstart[r] : 0;
+    int ix = 0, iy = 0;
+    if (SRC == kSrcDelta && n > 0) cell_xy(idx, g, inv_g, ix, iy);
     uint32_t word = 0;
     for (int s = 0; s < n; ++s) {
       const int64_t e = base + (int64_t)s * 32;
@@ -72,15 +76,19 @@ __device__ __forceinline__ void ray_segments(const DevGeom& G, const MatrixDev& 
         if ((s & 7) == 0) word = __ldcs(M.rcode + cbase + (int64_t)(s >> 3) * 32);
         if (s > 0) {
           const uint32_t code = (word >> (4 * (s & 7))) & 15u;
-          idx += (int)(code & 1u) + ((int)(code >> 1) - 1) * g;
+          const int dx = (int)(code & 1u), dy = (int)(code >> 1) - 1;
+          ix += dx;
+          iy += dy;
+          idx += dx + dy * g;
         }
       } else {
         idx = __ldcs(M.ridx + e);
+        cell_xy(idx, g, inv_g, ix, iy);
       }
       if constexpr (L16)
-        f(idx, 0.f, __ldcs(reinterpret_cast<const uint16_t*>(M.rlen) + e));
+        f(idx, ix, iy, 0.f, __ldcs(reinterpret_cast<const uint16_t*>(M.rlen) + e));
       else
-        f(idx, __ldcs(reinterpret_cast<const float*>(M.rlen) + e), (uint16_t)0);
+        f(idx, ix, iy, __ldcs(reinterpret_cast<const float*>(M.rlen) + e), (uint16_t)0);
     }
   }
 }
@@ -104,7 +112,6 @@ __global__ void __launch_bounds__(kTraceBlock)
                 uint16_t* run_lp, uint16_t* run_len, int* tile_count) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= (int64_t)G.P * G.C) return;
-  const int g = G.C;
   int64_t i = ray_run_off[r] - 1;
   int cur = -1, k = -1, len = 0, px = 0, py = 0;
   auto close = [&]() {
@@ -113,8 +120,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       key[i] = run_key(rk, cur, len, r, k);
     }
   };
-  ray_segments<SRC, false>(G, M, r, [&](int idx, float, uint16_t) {
-    const int ix = idx % g, iy = idx / g;
+  ray_segments<SRC, false>(G, M, r, [&](int, int ix, int iy, float, uint16_t) {
     const int t = tile_of(G, ix, iy, tiles_x);
     const bool step_ok = unit_step(ix, iy, px, py);
     px = ix;
@@ -162,7 +168,6 @@ __global__ void __launch_bounds__(kTraceBlock)
                 const int64_t* gcode_off, void* tlen, uint32_t* tcode) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= (int64_t)G.P * G.C) return;
-  const int g = G.C;
   int64_t i = ray_run_off[r] - 1;
   int cur = -1, s = 0, px = 0, py = 0;
   int64_t lbase = 0, cbase = 0;
@@ -201,8 +206,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       store(s >> 3);
     }
   };
-  ray_segments<SRC, L16>(G, M, r, [&](int idx, float l, uint16_t code) {
-    const int ix = idx % g, iy = idx / g;
+  ray_segments<SRC, L16>(G, M, r, [&](int, int ix, int iy, float l, uint16_t code) {
     const int t = tile_of(G, ix, iy, tiles_x);
     if (t != cur || !unit_step(ix, iy, px, py)) {
       flush();

@@ -27,11 +27,9 @@ __global__ void __launch_bounds__(kTraceBlock)
   float ml = 0.f;
   if (c < G.C) {
     if (ray_nruns) {
-      const int g = G.C;
       int runs = 0, cur = -1, px = 0, py = 0;
-      n = trace_ray(G, a, c, [&](int idx, float l, float) {
+      n = trace_ray(G, a, c, [&](int, float l, float, int ix, int iy) {
         ml = fmaxf(ml, l);
-        const int ix = idx % g, iy = idx / g;
         const int t = tile_of_pixel(ix, iy, tiles_x);
         if (t != cur || !unit_step(ix, iy, px, py)) {
           ++runs;
@@ -42,7 +40,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       });
       ray_nruns[(int64_t)a * G.C + c] = runs;
     } else {
-      n = trace_ray(G, a, c, [&](int, float l, float) { ml = fmaxf(ml, l); });
+      n = trace_ray(G, a, c, [&](int, float l, float, int, int) { ml = fmaxf(ml, l); });
     }
     nseg[(int64_t)a * G.C + c] = n;
   }
@@ -66,7 +64,6 @@ __global__ void __launch_bounds__(kTraceBlock)
   const int a = grp / G.gpa;
   const int c = (grp - a * G.gpa) * 32 + lane;
   if (c >= G.C) return;
-  const int g = G.C;
   const int64_t r = (int64_t)a * G.C + c;
   const int64_t base = M.roff[grp] + lane;
   const float4 coef = M.wcoef[a];
@@ -77,9 +74,8 @@ __global__ void __launch_bounds__(kTraceBlock)
   uint32_t word = 0;
   unsigned long long bad = 0;
   const bool store_fwd = rlen != nullptr;  // no forward matrix when traced on the fly
-  trace_ray(G, a, c, [&](int idx, float l, float l2) {
+  trace_ray(G, a, c, [&](int idx, float l, float l2, int ix, int iy) {
     const int64_t e = base + (int64_t)s * 32;
-    const int ix = idx % g, iy = idx / g;
     if (!store_fwd) {
     } else if (DELTA) {
       if (s == 0) {
@@ -152,11 +148,11 @@ __global__ void __launch_bounds__(kTraceBlock)
 
 // Total length through each pixel: the reference's replica[2p+1]
 // (sirt.cc:59), identical for every slice, so computed once.
-// HALF: the sum of the lengths each rounded to an IEEE half, as the
-// backprojection with half factors multiplies them (its total-length
-// normaliser, so that its lengths are one consistent set).
+// HALF: also Wh, the sum of the lengths each rounded to an IEEE half, as
+// the backprojection with half factors multiplies them (its total-length
+// normaliser, so that its lengths are one consistent set), in the same pass.
 template <bool L16, bool HALF>
-__global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W) {
+__global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W, float* Wh) {
   const int g = G.C;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)M.ntiles * 32) return;
@@ -165,7 +161,13 @@ __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W) {
   const int y = (tile / M.tiles_x) * 4 + (lane >> 3);
   if (x >= g || y >= g) return;
   const int64_t p = (int64_t)y * g + x;
-  float sum = 0.f, comp = 0.f;
+  float sum = 0.f, comp = 0.f, sumh = 0.f, comph = 0.f;
+  // compensated (Kahan) sum
+  auto kahan = [](float& s, float& cm, float l) {
+    const float yk = l - cm, tk = s + yk;
+    cm = (tk - s) - yk;
+    s = tk;
+  };
   for (int a = 0; a < G.P; ++a) {
     const int64_t pos = dense_pair(M.ntiles, a, tile, lane) * 2;
     float l0, l1;
@@ -180,32 +182,26 @@ __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W) {
       l1 = v.y;
     }
     if constexpr (HALF) {
-      l0 = __half2float(__float2half_rn(l0));
-      l1 = __half2float(__float2half_rn(l1));
+      kahan(sumh, comph, __half2float(__float2half_rn(l0)));
+      kahan(sumh, comph, __half2float(__float2half_rn(l1)));
     }
     if (exact) {
       sum = fadd(fadd(sum, l0), l1);
-    } else {  // compensated (Kahan) sum
-      float yk = l0 - comp, tk = sum + yk;
-      comp = (tk - sum) - yk;
-      sum = tk;
-      yk = l1 - comp;
-      tk = sum + yk;
-      comp = (tk - sum) - yk;
-      sum = tk;
+    } else {
+      kahan(sum, comp, l0);
+      kahan(sum, comp, l1);
     }
   }
   for_each_exception(M, tile, lane, [&](float l, int, int) {
-    if constexpr (HALF) l = __half2float(__float2half_rn(l));
+    if constexpr (HALF) kahan(sumh, comph, __half2float(__float2half_rn(l)));
     if (exact) {
       sum = fadd(sum, l);
     } else {
-      const float yk = l - comp, tk = sum + yk;
-      comp = (tk - sum) - yk;
-      sum = tk;
+      kahan(sum, comp, l);
     }
   });
   W[p] = sum;
+  if constexpr (HALF) Wh[p] = sumh;
 }
 
 __global__ void __launch_bounds__(kTraceBlock)
@@ -215,7 +211,7 @@ __global__ void __launch_bounds__(kTraceBlock)
   if (r >= nrays) return;
   const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
   int64_t o = offsets[r];
-  trace_ray(G, a, c, [&](int i, float l, float l2) {
+  trace_ray(G, a, c, [&](int i, float l, float l2, int, int) {
     idx[o] = i;
     len[o] = l;
     if (len2) len2[o] = l2;
@@ -261,18 +257,18 @@ void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
 }
 
 void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
-                    cudaStream_t st, bool half_lengths) {
+                    float* Wh, cudaStream_t st) {
   const int blocks = (int)(((int64_t)M.ntiles * 32 + 255) / 256);
   if (M.len_kind != LK_F32) {
-    if (half_lengths)
-      k_weights<true, true><<<blocks, 256, 0, st>>>(G, M, exact, W);
+    if (Wh)
+      k_weights<true, true><<<blocks, 256, 0, st>>>(G, M, exact, W, Wh);
     else
-      k_weights<true, false><<<blocks, 256, 0, st>>>(G, M, exact, W);
+      k_weights<true, false><<<blocks, 256, 0, st>>>(G, M, exact, W, Wh);
   } else {
-    if (half_lengths)
-      k_weights<false, true><<<blocks, 256, 0, st>>>(G, M, exact, W);
+    if (Wh)
+      k_weights<false, true><<<blocks, 256, 0, st>>>(G, M, exact, W, Wh);
     else
-      k_weights<false, false><<<blocks, 256, 0, st>>>(G, M, exact, W);
+      k_weights<false, false><<<blocks, 256, 0, st>>>(G, M, exact, W, Wh);
   }
 }
 
