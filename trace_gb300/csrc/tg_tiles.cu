@@ -17,9 +17,12 @@
 // batch. Summation order across runs is not fixed, so this path is used in
 // fast mode only.
 //
-// Construction (once per geometry): count runs per ray, emit run records
-// keyed by (tile, chunk-count class, ray, ordinal), radix-sort them (CUB),
-// pack each tile's runs into 32-lane groups, then trace again to fill the groups' streams.
+// Construction (once per geometry): runs per ray are counted by the tracing
+// pass that counts segments (k_trace_count); then run records keyed by
+// (tile, chunk-count class, ray, ordinal) are emitted, radix-sorted (CUB)
+// and packed into 32-lane groups per tile, and the groups' streams are
+// filled. Emission and fill walk each ray's segments in the stored
+// ray-ordered matrix, or trace the ray again when the plan keeps none.
 #include <cub/device/device_radix_sort.cuh>
 
 #include "tg_kernels.cuh"
