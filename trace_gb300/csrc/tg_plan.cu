@@ -372,17 +372,16 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
     seg_off[gi] = entries;
     code_off[gi] = words;
     entries += (int64_t)((steps[gi] + 7) / 8) * 256;  // chunks of 8 steps
-    words += (int64_t)((steps[gi] + 7) / 8) * 32;
+    words += (int64_t)((steps[gi] + 7) / 8) * 64;  // 8 step bytes per lane
   }
   const bool l16 = p->len_kind != TG_LEN_F32;
   int64_t *d_seg_off, *d_code_off;
   uint32_t* tcode;
   void* tlen = nullptr;
+  // unused steps keep the "stay" step 0 (tg_tiles.cu)
   if ((rc = dalloc(p, &d_seg_off, (size_t)groups)) || (rc = dalloc(p, &d_code_off, (size_t)groups)) ||
-      (rc = dalloc(p, &tcode, (size_t)words)))
+      (rc = dalloc(p, &tcode, (size_t)words, true)))
     return release(), rc;
-  // unused steps keep the "stay" code 2 in every nibble (tg_tiles.cu)
-  cudaMemsetAsync(tcode, 0x22, (size_t)words * sizeof(uint32_t), p->st);
   if (l16) {
     uint16_t* t;
     if ((rc = dalloc(p, &t, (size_t)entries, true))) return release(), rc;

@@ -8,7 +8,7 @@
 // tile's K-slice reconstruction into shared memory once and walks all runs
 // through it: lane = run, 32 runs of adjacent rays per warp. A lane's
 // lengths are stored in chunks of 8 consecutive steps (one 16-byte load per
-// 8 segments for 16-bit codes) with one word of 4-bit step codes per chunk,
+// 8 segments for 16-bit codes) with 8 bytes of step deltas per chunk,
 // chunks interleaved across the 32 lanes so each chunk load of a warp is one
 // contiguous 512-byte row; the next chunk is loaded while the current one is
 // consumed. A run's partial sum is added to its ray's sum with
@@ -35,10 +35,12 @@ constexpr int TS = kTileSide;     // tile side (pixels)
 constexpr int RS = TS + 1;        // shared-memory row stride (bank spread)
 constexpr int kBlock = 1024;      // forward: 32 warps per tile
 constexpr int kTraceBlock = 128;
-// 4-bit step codes are dx | (dy + 1) << 1; 2 = (0, 0), "stay", never a real
-// step. Every unused nibble of the tile stream holds it (a run's first step,
-// steps past a run's end, empty lanes), with a zero length.
-constexpr uint32_t kStayWord = 0x22222222u;
+// A step is stored as the signed byte dx + dy * RS, the change of the
+// shared-memory pixel index (dx in {0, 1}, dy in {-1, 0, 1}: -65 .. 66), so
+// the forward walks a run with one byte extraction and one add per step.
+// 0 is "stay", never a real step: every unused byte of the stream (a run's
+// first step, steps past a run's end, empty lanes) holds it, with a zero
+// length. Per lane and chunk the 8 bytes are one 8-byte word pair.
 
 __device__ __forceinline__ int tile_of(const DevGeom&, int ix, int iy, int tiles_x) {
   return tile_of_pixel(ix, iy, tiles_x);
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(kTraceBlock)
   int64_t i = ray_run_off[r] - 1;
   int cur = -1, s = 0, px = 0, py = 0;
   int64_t lbase = 0, cbase = 0;
-  uint32_t word = kStayWord;
+  uint32_t w0 = 0, w1 = 0;  // the chunk's step bytes (steps 0-3, 4-7)
   // the current chunk's 8 lengths as a shift register (oldest in the low
   // bits), stored whole: one 16-byte write per chunk and lane (32 for f32)
   uint32_t q[L16 ? 4 : 8] = {};
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       d[0] = make_uint4(q[0], q[1], q[2], q[3]);
       d[1] = make_uint4(q[4], q[5], q[6], q[7]);
     }
-    tcode[cbase + (int64_t)c * 32] = word;
+    *reinterpret_cast<uint2*>(tcode + cbase + (int64_t)c * 64) = make_uint2(w0, w1);
   };
   auto flush = [&]() {  // a run's last, partial chunk: zero lengths after it
     if (i >= ray_run_off[r] && (s & 7) != 0) {
@@ -216,19 +218,20 @@ __global__ void __launch_bounds__(kTraceBlock)
       ++i;
       cur = t;
       s = 0;
-      word = kStayWord;
+      w0 = w1 = 0;
       const int slot = run_slot[i];
       const int grp = slot >> 5, lane = slot & 31;
       lbase = gseg_off[grp] + lane * 8;
-      cbase = gcode_off[grp] + lane;
+      cbase = gcode_off[grp] + lane * 2;
     } else {
-      const int sh = 4 * (s & 7);
-      word = (word & ~(15u << sh)) | ((uint32_t)((ix - px) | ((iy - py + 1) << 1)) << sh);
+      const uint32_t b = (uint32_t)((ix - px) + (iy - py) * RS) & 0xffu;
+      if ((s & 7) < 4) w0 |= b << (8 * (s & 3));
+      else w1 |= b << (8 * (s & 3));
     }
     push(L16 ? (uint32_t)code : __float_as_uint(l));
     if ((s & 7) == 7) {
       store(s >> 3);
-      word = kStayWord;
+      w0 = w1 = 0;
     }
     px = ix;
     py = iy;
@@ -347,7 +350,7 @@ __device__ __forceinline__ void red_add(float* dst, const float (&acc)[K]) {
 template <int LK>
 struct Chunk {
   uint4 len[LK == LK_F32 ? 2 : 1];
-  uint32_t code;
+  uint2 code;  // step bytes
 };
 
 template <int LK>
@@ -362,7 +365,7 @@ __device__ __forceinline__ void load_chunk(const TileMatrixDev& T, int64_t lb,
     ch.len[0] = __ldcs(reinterpret_cast<const uint4*>(
         reinterpret_cast<const uint16_t*>(T.tlen) + lb + (int64_t)c * 256));
   }
-  ch.code = __ldcs(T.tcode + cb + (int64_t)c * 32);
+  ch.code = __ldcs(reinterpret_cast<const uint2*>(T.tcode + cb + (int64_t)c * 64));
 }
 
 template <int LK>
@@ -408,7 +411,7 @@ __global__ void __launch_bounds__(kBlock)
     int si = (lp / TS) * RS + lp % TS;  // shared-memory index of the current pixel
     const int chunks = (T.gsteps[grp] + 7) >> 3;
     const int64_t lb = T.gseg_off[grp] + lane * 8;
-    const int64_t cb = T.gcode_off[grp] + lane;
+    const int64_t cb = T.gcode_off[grp] + lane * 2;
     float acc[K];
 #pragma unroll
     for (int j = 0; j < K; ++j) acc[j] = 0.f;
@@ -417,12 +420,11 @@ __global__ void __launch_bounds__(kBlock)
     for (int c = 0; c < chunks; ++c) {
       if (c + 1 < chunks) load_chunk<LK>(T, lb, cb, c + 1, nxt);
       // No per-step guard: a run's first step and every step past its end
-      // carry the "stay" code and a zero length (see k_runs_fill), so
+      // carry the "stay" step 0 and a zero length (see k_runs_fill), so
       // lanes of shorter runs add 0 * (a finite pixel value) in place.
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        const uint32_t code = (cur.code >> (4 * j)) & 15u;
-        si += (int)(code & 1u) + ((int)(code >> 1) - 1) * RS;
+        si += (int)(int8_t)((j < 4 ? cur.code.x : cur.code.y) >> (8 * (j & 3)));
         if constexpr (H)
           tile_fma_half<K>(smh, si, chunk_len<LK>(cur, j, inv_scale), acc);
         else
