@@ -108,14 +108,21 @@ typedef struct {
                              halves with FP32 arithmetic - the forward
                              projection's shared-memory reconstruction tile,
                              and (MLEM/PML/APMLR) the per-ray factors as
-                             factor - 1 - halving the bytes of both gathers */
+                             factor - 1 - halving the bytes of both gathers;
+                             the backward matrix then stores its lengths as
+                             halves (16-bit storages). tg_reduce keeps FP32
+                             factors (half tile) */
   int forward_on_the_fly; /* not with FP64 mode: no ray-ordered forward matrix
                              is stored; the forward projections that would
-                             read it (tg_reduce, tg_forward_project, and
-                             tg_iterate without forward_tiles) trace each ray
-                             while projecting it. Saves the matrix's memory
-                             (segments x (L + 4) bytes) for tracing work;
-                             results equal the stored f32 form's */
+                             read it (tg_iterate, tg_reduce and
+                             tg_forward_project on plans without
+                             forward_tiles) trace each ray while projecting
+                             it. Saves the matrix's memory (segments x
+                             (L + 4) bytes) for tracing work; results equal
+                             the stored f32 form's. With forward_tiles the
+                             projections use the tile-ordered matrix and the
+                             option only saves memory (the tile build traces
+                             instead of reading the ray-ordered matrix) */
 } tg_plan_desc;
 
 typedef struct {

@@ -95,3 +95,37 @@ def test_driver_builds_and_rejects_bad_usage(lib):
                         "-o", "/tmp/x", "-P", "4", "-S", "1", "-C", "8"],
                        capture_output=True, text=True)
     assert r.returncode == 1 and "cannot open" in r.stderr
+
+
+def test_ctypes_structures_match_the_header(tmp_path):
+    """The Python binding's ctypes structures have the C header's layout:
+    size and every field's offset, as a C compiler lays them out."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"tg_plan_desc": tg.PlanDesc, "tg_params": tg.Params,
+               "tg_plan_info": tg.PlanInfo, "tg_timing": tg.Timing}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "trace_gb300.h"',
+             'int main(void) {']
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    got = {}
+    for line in out.split("\n"):
+        if line:
+            cname, field, val = line.split()
+            got[(cname, field)] = int(val)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
