@@ -59,23 +59,23 @@ METRIC = ("slice-iter/s at 2048²×1500 angles, mixed+batched vs plain "
 WORKLOADS = {
     # the headline workload
     "pml2048": dict(alg="pml", C=2048, P=1500, S=128, iters=30, beta=0.05, texture=0.02,
-                    plain_slices=8, fp64_slices=1, name=(
+                    plain_slices=8, fp64_slices=8, name=(
                         "PML 8-neighbour quadratic penalty beta=0.05, 2048x2048 grid, "
                         "128 slices, 1500 angles x 2048 columns, 30 iterations")),
     # a small case of the same kernels, for profiling captures and quick runs
     "pml1024": dict(alg="pml", C=1024, P=720, S=8, iters=30, beta=0.05, texture=0.02,
-                    plain_slices=8, fp64_slices=1, name=(
+                    plain_slices=8, fp64_slices=8, name=(
                         "PML beta=0.05, 1024x1024 grid, 8 slices, 720 angles")),
     "sirt256": dict(alg="sirt", C=256, P=180, S=8, iters=10, i0=1e4,
                     plain_slices=8, fp64_slices=8, name=(
                         "SIRT, 256x256 grid, 8 slices, 180 angles x 256 columns, "
                         "10 iterations, Poisson noise I0=1e4")),
     "mlem1024": dict(alg="mlem", C=1024, P=720, S=64, iters=20, i0=5e3, clip=1e-6,
-                     plain_slices=8, fp64_slices=2, name=(
+                     plain_slices=8, fp64_slices=8, name=(
                          "MLEM, 1024x1024 grid, 64 slices, 720 angles x 1024 columns, "
                          "20 iterations, Poisson noise I0=5e3, sinogram clipped at 1e-6")),
     "apmlr2048": dict(alg="apmlr", C=2048, P=1500, S=2048, iters=25, beta=0.02, i0=2e4,
-                      volume=True, plain_slices=8, fp64_slices=4, name=(
+                      volume=True, plain_slices=8, fp64_slices=8, name=(
                           "APMLR 8-neighbour regulariser beta0=0.02 (beta1, delta0, "
                           "delta1, regw 1), full volume 2048 slices x 2048x2048 grid, "
                           "1500 angles x 2048 columns, 25 iterations, random-ellipsoid "
@@ -386,8 +386,8 @@ def format_bytes(info, W, K, tiles, half=False):
     fb = 2 if half and W["alg"] != "sirt" else 4  # factor bytes per ray and slice
     C, P = W["C"], W["P"]
     R, g2 = P * C, C * C
-    if tiles:  # tile stream + one read of the batch + the ray sums written
-        fwd = info["tile_bytes"] + 4 * g2 * K + 4 * R * K
+    if tiles:  # tile stream + one read of the batch + the runs' partial sums written
+        fwd = info["tile_bytes"] + 4 * g2 * K + 4 * info["partial_slots"] * K
     else:      # matrix + sinogram in, factors out, batch read once
         fwd = info["forward_bytes"] + 4 * R * K * 2 + 4 * g2 * K
     back = (info["backward_bytes"] + fb * R * K + 4 * g2 * K * 2 + 4 * g2
@@ -455,16 +455,21 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     sino = make_data(W, dev, plan)
     upload(plan, W, sino)
     plan.reset_recon(alg)
+    # each iteration replays a captured CUDA graph (captured in the warm-up)
+    plan.set_graphs(args.graphs)
     for _ in range(args.warmup):
         plan.iterate(alg, 1, prm)
     torch.cuda.synchronize()
     barrier(ws)
     torch.cuda.synchronize()
-    plan.set_timing(True)
     with ClockSampler(local) as clk:
         ms = time_iterations(plan, alg, prm, args.steps, stream, torch)
     torch.cuda.synchronize()
     barrier(ws)
+    # per-kernel device times from a separate pass after the timed region
+    # (the per-launch timers run eagerly, outside any graph)
+    plan.set_timing(True)
+    time_iterations(plan, alg, prm, max(2, min(args.steps, 3)), stream, torch)
     tim = plan.timing()
     plan.set_timing(False)
     ms_max = max_over_ranks(ms, ws)
@@ -492,6 +497,10 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
         "frac": achieved / hbm_peak, "peak_kind": f"{peak_kind} (burst copy)",
         "traffic": traffic, "kernel": kname,
+        # the same kernel's measured DRAM bytes (ncu, one launch of this
+        # configuration) over its live launch time: what HBM actually moved
+        "achieved_traffic": gbs(traffic, dom_ms) if traffic else None,
+        "frac_traffic": gbs(traffic, dom_ms) / hbm_peak if traffic else None,
         "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": dom_ms,
         "bytes_definition": "segments x (4 + L) per matrix pass + per-slice "
                             "sinogram/reconstruction/penalty bytes x K",
@@ -501,7 +510,9 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
             ("k_forward_tiled" if args.tiles else "k_forward"): {
                 "avg_ms": fwd_avg, "bytes": fwd_b, "gbs": gbs(fwd_b, fwd_avg),
                 "format_bytes": fwd_f, "format_gbs": gbs(fwd_f, fwd_avg)},
-            "k_fwd_finish": {"avg_ms": tim["other_ms"] / max(tim["other_launches"], 1)},
+            "k_fwd_finish": {"avg_ms": tim["other_ms"] / max(tim["other_launches"], 1),
+                             "format_bytes": 4 * info["partial_slots"] * K
+                                             + 4 * W["P"] * W["C"] * K * 2},
             "k_backward": {"avg_ms": back_avg, "bytes": back_b, "gbs": gbs(back_b, back_avg),
                            "format_bytes": back_f, "format_gbs": gbs(back_f, back_avg)},
         },
@@ -518,9 +529,12 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     if args.fp64_check and rank == 0:
         rel = fp64_check(args, W, theta, sino, prm, tg, torch, dev)
 
-    # ---- plain FP32 path (f32 lengths, 1 slice per pass, reference op order)
-    plain = None
+    # ---- FP32 on the measured schedule, and the plain FP32 path (f32
+    # lengths, 1 slice per pass, reference operation order)
+    plain = same = None
     if args.plain and rank == 0:
+        same = fp32_same_schedule(args, W, theta, sino, prm, tg, torch, stream)
+        torch.cuda.empty_cache()
         plain = plain_path(args, W, theta, sino, prm, tg, torch, stream)
 
     # ---- end to end through the C ABI with host buffers
@@ -550,6 +564,7 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
                    "forward": "tile-staged (64x64 shared-memory tiles)" if args.tiles
                               else "ray-ordered",
                    "step": f"one {alg.upper()} iteration over all {S} slices",
+                   "graphs": bool(args.graphs),
                    "l2": "inputs larger than L2 (system matrix "
                          f"{(info['forward_bytes'] + info['backward_bytes']) / 1e9:.1f} GB "
                          "streamed per step)",
@@ -557,28 +572,52 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
         "roofline": roofline, "clocks": clk.summary(), "gpu_launches": launches,
         "setup_ms": info["setup_ms"], "num_segments_per_slice": info["num_segments"],
         "device_bytes": info["device_bytes"],
-        "rel_l2_vs_fp64": rel, "plain_fp32": plain, "e2e": e2e, "autotune": tuned,
+        "rel_l2_vs_fp64": rel, "plain_fp32": plain, "fp32_same_schedule": same,
+        "mixed_vs_fp32_same_schedule": value / same["value"] if same else None,
+        "mixed_vs_plain_fp32": value / plain["value"] if plain else None,
+        "e2e": e2e, "autotune": tuned,
         "cpu_baseline": cpu,
         "wall_s": time.time() - t0,
     }
     print(json.dumps(line), flush=True)
 
 
-def fp64_check(args, W, theta, sino, prm, tg, torch, dev):
-    """Per-iteration relative L2 against the GPU FP64 mode on a slice subset,
-    over the workload's full iteration count, for the mixed path (its
-    arithmetic per slice does not depend on the slices per pass) and the
-    plain FP32 path (the reference's operation order)."""
+def fp64_slice_subset(W):
+    """Indices of the slices the FP64 comparison runs: spread evenly over the
+    volume for the slice-independent algorithms; for APMLR, whose slices are
+    coupled by the axial penalty, one contiguous block from the middle (run
+    as its own sub-volume by every configuration compared)."""
     import numpy as np
-    n = W["fp64_slices"]
-    sub = sino[:, :n, :].contiguous()
+    n, S = W["fp64_slices"], W["S"]
+    if n >= S:
+        return list(range(S))
+    if W["alg"] == "apmlr":
+        s0 = (S - n) // 2
+        return list(range(s0, s0 + n))
+    return sorted(set(int(round(x)) for x in np.linspace(0, S - 1, n)))
+
+
+def fp64_check(args, W, theta, sino, prm, tg, torch, dev):
+    """Per-iteration relative L2 against the GPU FP64 mode on a slice subset
+    (fp64_slice_subset), over the workload's full iteration count, for the
+    mixed path as measured (its arithmetic per slice does not depend on the
+    slices per pass), the FP32 path on the same schedule (f32 lengths and
+    gather operands, same slices per pass and forward) and the plain FP32
+    path (the reference's operation order)."""
+    import numpy as np
+    idx = fp64_slice_subset(W)
+    n = len(idx)
+    sub = sino[:, idx, :].contiguous()
     configs = {
         "fp64": dict(len_storage="f32", mode="fp64"),
         # the measured configuration, same kernels (same slices per pass: the
-        # subset fills part of one batch)
+        # subset fills one batch)
         "mixed": dict(len_storage=args.len_storage, mode="fast", delta_index=True,
                       forward_tiles=args.tiles, backward_staged=args.staged,
                       half_gathers=args.half, slices_per_pass=args.slices_per_pass),
+        "fp32_same_schedule": dict(len_storage="f32", mode="fast", delta_index=True,
+                                   forward_tiles=args.tiles, backward_staged=args.staged,
+                                   slices_per_pass=args.slices_per_pass),
         "plain_fp32": dict(len_storage="f32", mode="exact"),
     }
     runs = {}
@@ -594,15 +633,49 @@ def fp64_check(args, W, theta, sino, prm, tg, torch, dev):
             snaps.append(p.get_recon(alg))
         runs[key] = snaps
         p.close()
-    out = {"slices": n, "iterations": W["iters"], "reference": "GPU FP64 mode"}
-    for key in ("mixed", "plain_fp32"):
+        torch.cuda.empty_cache()
+    out = {"slices": n, "slice_indices": idx, "iterations": W["iters"],
+           "reference": "GPU FP64 mode (pinned to the CPU FP64 oracle by the -m gpu tests)"}
+    for key in ("mixed", "fp32_same_schedule", "plain_fp32"):
         errs = [float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b))
                 for a, b in zip(runs[key], runs["fp64"])]
         out[key] = {"max": max(errs), "final": errs[-1], "per_iteration": errs}
     return out
 
 
+def fp32_same_schedule(args, W, theta, sino, prm, tg, torch, stream):
+    """The FP32 GPU path on the measured schedule: f32 lengths and FP32
+    gather operands, with the same slices per pass, forward projection,
+    backprojection and CUDA graphs as the mixed path, over the workload's
+    slices (at most 256 of a full volume)."""
+    n = min(W["S"], 256)
+    sub = sino[:, :n, :].contiguous() if n < W["S"] else sino
+    p = tg.Plan(W["P"], n, W["C"], theta, len_storage="f32",
+                slices_per_pass=args.slices_per_pass, mode="fast", delta_index=True,
+                forward_tiles=args.tiles, backward_staged=args.staged,
+                forward_on_the_fly=args.otf)
+    p.set_stream(stream)
+    p.set_graphs(True)
+    info = p.info()
+    alg = W["alg"]
+    upload(p, W, sub)
+    p.reset_recon(alg)
+    for _ in range(args.warmup):
+        p.iterate(alg, 1, prm)
+    torch.cuda.synchronize()
+    ms = time_iterations(p, alg, prm, args.steps, stream, torch)
+    p.close()
+    return {"value": n * args.steps / (ms / 1000.0), "unit": "slice-iter/s",
+            "slices": n, "steps": args.steps, "setup_ms": info["setup_ms"],
+            "matrix_bytes": info["forward_bytes"] + info["backward_bytes"] + info["tile_bytes"],
+            "config": f"f32 lengths, FP32 gather operands, {args.slices_per_pass} slices "
+                      "per pass, " + ("tile-staged forward" if args.tiles else
+                                      "ray-ordered forward") + ", CUDA graphs"}
+
+
 def plain_path(args, W, theta, sino, prm, tg, torch, stream):
+    """The plain FP32 path in the reference's operation order: f32 lengths,
+    int32 indices, one slice per matrix pass, exact arithmetic."""
     n = W["plain_slices"]
     sub = sino[:, :n, :].contiguous()
     p = tg.Plan(W["P"], n, W["C"], theta, len_storage="f32", slices_per_pass=1,
@@ -621,8 +694,8 @@ def plain_path(args, W, theta, sino, prm, tg, torch, stream):
     return {"value": n * steps / (ms / 1000.0), "unit": "slice-iter/s",
             "slices": n, "steps": steps, "setup_ms": info["setup_ms"],
             "matrix_bytes": info["forward_bytes"] + info["backward_bytes"],
-            "config": "f32 lengths, explicit int32 indices, 1 slice per pass, "
-                      "reference operation order"}
+            "config": "reference operation order: f32 lengths, explicit int32 indices, "
+                      "1 slice per pass, IEEE-rounded mul/add/div"}
 
 
 def end_to_end(args, W, theta, sino, prm, tg, torch, stream):
@@ -643,6 +716,7 @@ def end_to_end(args, W, theta, sino, prm, tg, torch, stream):
                     delta_index=True, forward_tiles=args.tiles,
                     backward_staged=args.staged, half_gathers=args.half)
         p.set_stream(stream)
+        p.set_graphs(args.graphs)
         upload(p, W, host)
         p.reset_recon(W["alg"])
         p.iterate(W["alg"], W["iters"], prm)
@@ -868,6 +942,8 @@ def main():
     ap.add_argument("--autotune", action="store_true",
                     help="time the plan configurations on a 16-slice sample first "
                          "and run the fastest")
+    ap.add_argument("--no-graphs", dest="graphs", action="store_false",
+                    help="eager launches instead of one CUDA graph per iteration")
     ap.add_argument("--no-plain", dest="plain", action="store_false")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")

@@ -110,8 +110,11 @@ typedef struct {
                              and (MLEM/PML/APMLR) the per-ray factors as
                              factor - 1 - halving the bytes of both gathers;
                              the backward matrix then stores its lengths as
-                             halves (16-bit storages). tg_reduce keeps FP32
-                             factors (half tile) */
+                             halves (16-bit storages). The first iteration
+                             after tg_reset_recon / tg_set_recon keeps FP32
+                             factors (they start far from 1, where a half of
+                             factor - 1 is least precise). tg_reduce keeps
+                             FP32 factors (half tile) */
   int forward_on_the_fly; /* not with FP64 mode: no ray-ordered forward matrix
                              is stored; the forward projections that would
                              read it (tg_iterate, tg_reduce and
@@ -123,6 +126,12 @@ typedef struct {
                              projections use the tile-ordered matrix and the
                              option only saves memory (the tile build traces
                              instead of reading the ray-ordered matrix) */
+  int compensated;        /* fast mode with forward_tiles and the L1
+                             backprojection: compensated (Kahan) summation -
+                             each ray's sum in blocks of 8 segments within a
+                             tile run and across its runs, each pixel's
+                             backprojection sum in blocks of 4 angles; the
+                             blocks themselves are FMA chains */
 } tg_plan_desc;
 
 typedef struct {
@@ -151,6 +160,10 @@ typedef struct {
   int forward_traced;         /* 1: the ray-ordered forward projection traces
                                  its rays on the fly - requested, or a stray
                                  segment's step did not fit the 4-bit code */
+  int64_t partial_slots;      /* tile-staged forward: slots of the runs'
+                                 partial sums (slices_per_pass floats each),
+                                 written by every forward launch and summed
+                                 per ray in a fixed order */
 } tg_plan_info;
 
 typedef struct {
@@ -267,18 +280,26 @@ int tg_trace_rays(tg_plan* plan, int32_t* counts, const int64_t* offsets,
  *
  *   recon: device, C x C floats - the reconstruction the forward projection
  *          reads (for APMLR's reference behaviour, slice s-1).
- *   sino:  device, P x C floats - this slice's sinogram rows (|x| applied
- *          where the driver applies it).
+ *   sino:  device, P x C floats - this slice's sinogram rows, used as they
+ *          are: the caller applies |x| where the driver applies it
+ *          (trace_utils::Absolute) and any floor it wants (what
+ *          tg_set_sinogram_clip applies on upload is not applied here).
  *   num:   device, C x C floats - receives replica[2p] for every pixel, the
  *          values tg_get_replica returns at even positions.
  * The per-ray factors between the two passes live in one file-scope device
  * array of 4,194,304 floats (16 MiB, held by every GPU that loads the
  * library until the process exits); plans with P*C above that return
- * TG_E_LIMIT. The first call on a device looks the array's address up
- * (cudaGetSymbolAddress) and caches it, so make that first call before any
- * stream capture. Every call shares the array: calls whose work overlaps on
- * the GPU (different streams, or different plans on one device) race on it;
- * the array needs no clearing, since each call writes every factor it reads.
+ * TG_E_LIMIT. tg_plan_create looks the array's device address up
+ * (cudaGetSymbolAddress, in the plan's context) and keeps it in the plan, so
+ * calls look nothing up and the address is valid for the plan's lifetime.
+ * Every call shares the array: calls whose work overlaps on the GPU
+ * (different streams, or different plans on one device) race on it; the
+ * array needs no clearing, since each call writes every factor it reads.
+ * The forward projection is always the ray-ordered one (or the on-the-fly
+ * tracer when the plan keeps no ray-ordered matrix) and the backprojection
+ * the L1 one with FP32 factors, whatever the plan's forward_tiles /
+ * backward_staged / half_gathers options, so on such plans the numerators
+ * agree with tg_reduce's to the rounding of those options' operands.
  * Work is issued on the plan's stream; the device that was current when the
  * plan was created must be current. */
 int tg_reduce_slice_noalloc(tg_plan* plan, int alg, const tg_params* params,

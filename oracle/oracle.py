@@ -23,7 +23,8 @@ PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
 # for timing the CPU baseline only
 PORT_FAST_SO = os.path.join(HERE, "_build", "liboracle_fastmath.so")
 REF_SO = os.path.join(HERE, "_ref", "libtrace_ref.so")
-REF_SRC = os.environ.get("TRACE_REFERENCE_DIR", "/root/reference")
+# the reference checkout, given by the environment (no default location)
+REF_SRC = os.environ.get("TRACE_REFERENCE_DIR", "")
 
 SIRT, MLEM, PML, APMLR = 0, 1, 2, 3
 ALGS = {"sirt": SIRT, "mlem": MLEM, "pml": PML, "apmlr": APMLR}
@@ -37,8 +38,9 @@ def build_port(quiet: bool = True) -> str:
 
 
 def build_ref(quiet: bool = True) -> str | None:
-    """Compile the reference sources into _ref/ (None if they are absent)."""
-    if not os.path.isdir(os.path.join(REF_SRC, "src", "common")):
+    """Compile the reference sources named by TRACE_REFERENCE_DIR into _ref/
+    (None when the variable is unset or names no reference checkout)."""
+    if not REF_SRC or not os.path.isdir(os.path.join(REF_SRC, "src", "common")):
         return None
     subprocess.run(["make", "-s", "-j8", "ref", f"REF={REF_SRC}"], cwd=HERE,
                    check=True, stdout=subprocess.DEVNULL if quiet else None)

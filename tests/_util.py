@@ -40,3 +40,22 @@ def ellipse_sino(C, P, S, seed, tabs=None, center=0.0):
         tabs = O.angle_table(th)
     sim = O.forward(ph, tabs, center)
     return th, tabs, ph, sim
+
+
+# SIRT at the first benchmark geometry: 256 x 256 grid, 8 slices, 180 angles
+# x 256 columns, 10 iterations; seeded random-ellipse phantoms projected by
+# the oracle's projector (bit-identical to the reference's ray sum), Poisson
+# counts at I0 = 1e4 converted with -log.
+CONFIG1 = dict(C=256, P=180, S=8, n_iter=10, i0=1e4, phantom_seed=101, noise_seed=202)
+
+
+def config1_data():
+    """(theta, angle tables, sinogram [P][S][C]) of the SIRT 256 workload."""
+    from trace_gb300.phantom import ellipse_phantoms, poisson_log
+    c = CONFIG1
+    th = theta_uniform(c["P"])
+    tabs = O.angle_table(th)
+    ph = ellipse_phantoms(c["C"], c["S"], seed=c["phantom_seed"])
+    sim = O.forward(ph, tabs, threads=8)  # each ray summed sequentially
+    sino = poisson_log(sim, c["i0"], seed=c["noise_seed"], g=c["C"])
+    return th, tabs, sino

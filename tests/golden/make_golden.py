@@ -3,10 +3,10 @@
 Runs the reference's own tracer, operators and DISP engine, compiled
 unmodified from the reference tree by ``oracle/Makefile`` (target ``ref``)
 with one reduction thread (the only bit-reproducible setting of its engine).
-Needs the reference sources (TRACE_REFERENCE_DIR, default the read-only
-mount); the fixtures it writes are what the tests use everywhere else.
+Needs the reference sources: TRACE_REFERENCE_DIR names the checkout; the
+fixtures it writes are what the tests use everywhere else.
 
-    python tests/golden/make_golden.py
+    TRACE_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -61,6 +61,23 @@ def recon_fixture(name, alg, C, P, S, n_iter, seed, center=0.0, **params):
     print(name, alg, "ok")
 
 
+def config1_fixture(name):
+    """Hashes of the reference's SIRT run at the 256 x 256, 180-angle,
+    8-slice, 10-iteration workload with Poisson data (the input is rebuilt by
+    tests._util.config1_data; its hash is stored to catch generator drift)."""
+    import json
+    from tests._util import CONFIG1, config1_data
+    th, _, sino = config1_data()
+    r = O.ref_run("sirt", sino, th, n_iter=CONFIG1["n_iter"], want_iters=True)
+    d = dict(CONFIG1, sha_sino=sha(sino),
+             sha_iters=[sha(r["iters"][i]) for i in range(CONFIG1["n_iter"])],
+             norm_iters=[float(np.linalg.norm(r["iters"][i].astype(np.float64)))
+                         for i in range(CONFIG1["n_iter"])])
+    with open(os.path.join(HERE, name), "w") as f:
+        json.dump(d, f, indent=1)
+    print(name, "ok")
+
+
 def main():
     if O.build_ref() is None:
         raise SystemExit("reference sources not available")
@@ -78,6 +95,7 @@ def main():
     recon_fixture("recon_apmlr_s1.npz", "apmlr", 20, 16, 1, 2, seed=15)
     recon_fixture("recon_pml_odd.npz", "pml", 21, 13, 2, 2, seed=16, beta=2.0,
                   center=9.7)
+    config1_fixture("config1_sirt256.json")
 
 
 if __name__ == "__main__":

@@ -47,5 +47,5 @@ def test_driver_matches_oracle(tmp_path, alg, extra, params):
     halo = 1 if alg == "apmlr" else 0
     got = np.fromfile(of, np.float32).reshape(S + 2 * halo, C, C)
     want = O.run(alg, sino, theta=th, n_iter=n, **params)["recon"]
-    tol = (2e-4 if "--half" in extra else 1e-4) if "--fast" in extra else 2e-6
+    tol = 1e-4 if "--fast" in extra else 2e-6
     assert rel_l2(got, want) < tol

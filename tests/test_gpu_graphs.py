@@ -1,5 +1,6 @@
 """CUDA-graph replay of iterations and batches of independent plans: the
-results must be bit-identical to plain launches (exact mode)."""
+results must be bit-identical to plain launches, in exact mode and on the
+tile-staged fast path (no atomics: every launch sums in the same order)."""
 import numpy as np
 import pytest
 
@@ -32,10 +33,8 @@ def test_graph_replay_identical(alg, kw):
         plan.iterate(alg, 2, prm)  # parity flips between calls
         outs.append(plan.get_recon(alg))
         plan.close()
-    if kw.get("forward_tiles"):  # ray sums arrive by atomics: order may vary
-        assert np.max(np.abs(outs[1] - outs[0])) <= 1e-5 * np.max(np.abs(outs[0]))
-    else:
-        assert np.array_equal(bits(outs[0]), bits(outs[1]))
+    # the tile-staged forward adds each ray's run sums in a fixed order
+    assert np.array_equal(bits(outs[0]), bits(outs[1]))
 
 
 def test_batch_matches_individual_plans():

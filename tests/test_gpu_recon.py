@@ -273,5 +273,5 @@ def test_many_angles(P):
     plan.set_sinogram(sino, apply_abs=True)
     plan.reset_recon("mlem")
     plan.iterate("mlem", it)
-    assert rel_l2(plan.get_recon("mlem"), ref) < 2e-4
+    assert rel_l2(plan.get_recon("mlem"), ref) < 1e-4
     plan.close()

@@ -65,8 +65,9 @@ def test_half_gathers_against_fp64(alg, K, S):
     """16-bit gather operands (shared-memory tile and ratio factors as halves,
     FP32 arithmetic): error against the FP64 oracle stays at the level of the
     16-bit lengths. Small grids converge from far away in few iterations, the
-    loosest case for half factors (rel-L2 bound 2e-4 here; the 2048^2 x 1500
-    workload's 30-iteration error is measured by the benchmark)."""
+    loosest case for half factors (rel-L2 bound 1e-4 here; the 2048^2 x 1500
+    workload's 30-iteration error is measured by the benchmark). The first
+    iteration keeps FP32 factors."""
     C, P, it = 96, 72, 6
     th = theta_uniform(P)
     tabs = O.angle_table(th)
@@ -85,7 +86,7 @@ def test_half_gathers_against_fp64(alg, K, S):
         errs[half] = rel_l2(plan.get_recon(alg), ref)
         plan.close()
     assert errs[False] < 1e-4, errs
-    assert errs[True] < 2e-4, errs
+    assert errs[True] < 1e-4, errs
 
 
 def test_half_gathers_keep_operator_path_fp32():
@@ -135,8 +136,8 @@ def test_sixteen_slices_per_pass_match_eight(alg):
         plan.iterate(alg, 4, prm)
         outs.append(plan.get_recon(alg))
         plan.close()
-    # same arithmetic per slice; the run sums are added in a different order
-    assert rel_l2(outs[1], outs[0]) < 1e-6
+    # same arithmetic and summation order per slice
+    assert np.array_equal(bits(outs[1]), bits(outs[0]))
 
 
 def test_sixteen_slices_with_tiles_need_half_gathers():
@@ -164,14 +165,15 @@ def test_half_gathers_with_each_length_storage(storage):
     plan.iterate("mlem", it, tg.default_params("mlem"))
     err = rel_l2(plan.get_recon("mlem"), ref)
     plan.close()
-    assert err < (3e-3 if storage == "bf16" else 2e-4), err
+    assert err < (3e-3 if storage == "bf16" else 1e-4), err
 
 
 @pytest.mark.parametrize("alg", ["sirt", "mlem", "pml", "apmlr"])
 def test_operator_path_uses_tiles(alg):
     """reduce -> replica and forward_project on a tile-ordered plan agree with
-    the ray-ordered plan of the same storage (sums by atomics: relative
-    L2 <= 1e-6), as the drivers' RunParallelReduction / UpdateRecon loop
+    the ray-ordered plan of the same storage (ray sums regrouped by tile
+    runs: relative L2 <= 1e-6), as the drivers' RunParallelReduction /
+    UpdateRecon loop
     calls them."""
     C, P, S = 72, 54, 6
     th = theta_uniform(P)

@@ -90,7 +90,7 @@ def test_forward_and_fg_helpers_consistent():
     assert np.array_equal(bits(new), bits(f["iters"][-1]))
 
 
-@pytest.mark.skipif(O.build_ref() is None, reason="reference sources unavailable")
+@pytest.mark.skipif(O.ref() is None, reason="the compiled reference (oracle/_ref) is unavailable")
 def test_oracle_vs_reference_fresh_random_case():
     rng = np.random.default_rng(99)
     C, P, S = 40, 33, 2
@@ -103,3 +103,24 @@ def test_oracle_vs_reference_fresh_random_case():
         r = O.ref_run(alg, sino, th, n_iter=2, beta=1.5)
         m = O.run(alg, sino, tables=tabs, n_iter=2, beta=1.5)
         assert np.array_equal(bits(r["recon"]), bits(m["recon"])), alg
+
+
+def test_oracle_pinned_at_sirt256_workload():
+    """The oracle reproduces the compiled reference bit for bit at the
+    SIRT 256 x 256, 180-angle, 8-slice, 10-iteration workload with Poisson
+    data (tests/golden/config1_sirt256.json, made by make_golden.py)."""
+    import hashlib
+    import json
+    import os
+
+    from tests._util import GOLDEN, config1_data
+    with open(os.path.join(GOLDEN, "config1_sirt256.json")) as f:
+        g = json.load(f)
+
+    def sha(a):
+        return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+    _, tabs, sino = config1_data()
+    assert sha(sino) == g["sha_sino"], "input generator changed"
+    r = O.run("sirt", sino, tables=tabs, n_iter=g["n_iter"], threads=1, want_iters=True)
+    assert [sha(r["iters"][i]) for i in range(g["n_iter"])] == g["sha_iters"]

@@ -55,7 +55,7 @@ class PlanDesc(C.Structure):
                 ("mode", C.c_int), ("delta_index", C.c_int),
                 ("apmlr_fixed_offset", C.c_int), ("forward_tiles", C.c_int),
                 ("backward_staged", C.c_int), ("half_gathers", C.c_int),
-                ("forward_on_the_fly", C.c_int)]
+                ("forward_on_the_fly", C.c_int), ("compensated", C.c_int)]
 
 
 class Params(C.Structure):
@@ -69,7 +69,7 @@ class PlanInfo(C.Structure):
                 ("max_segment_length", C.c_float), ("setup_ms", C.c_double),
                 ("batches", C.c_int), ("tile_bytes", C.c_int64),
                 ("tile_runs", C.c_int64), ("window_exceptions", C.c_int64),
-                ("forward_traced", C.c_int)]
+                ("forward_traced", C.c_int), ("partial_slots", C.c_int64)]
 
 
 class Timing(C.Structure):
@@ -133,7 +133,7 @@ class Plan:
                  delta_index=False, apmlr_fixed_offset=False, slice_id=0,
                  num_total_slices=None, sin_tab=None, cos_tab=None,
                  forward_tiles=False, backward_staged=False, half_gathers=False,
-                 forward_on_the_fly=False):
+                 forward_on_the_fly=False, compensated=False):
         self._lib = load_library()
         self.P, self.S, self.C = int(num_projs), int(num_slices), int(num_cols)
         d = PlanDesc(self.P, self.S, self.C, float(center), int(slice_id),
@@ -143,7 +143,8 @@ class Plan:
                      MODES[mode] if isinstance(mode, str) else int(mode),
                      int(bool(delta_index)), int(bool(apmlr_fixed_offset)),
                      int(bool(forward_tiles)), int(bool(backward_staged)),
-                     int(bool(half_gathers)), int(bool(forward_on_the_fly)))
+                     int(bool(half_gathers)), int(bool(forward_on_the_fly)),
+                     int(bool(compensated)))
         theta = np.ascontiguousarray(theta, np.float32)
         if theta.size != self.P:
             raise ValueError("theta must have num_projs entries")

@@ -160,8 +160,17 @@ __device__ __forceinline__ void accumulate(float (&acc)[K], const float (&rf)[K]
   }
 }
 
-template <int K, int LK, bool EXACT, bool PEN, bool FH>
-__global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
+// Resident blocks per SM for each variant: compensated sums keep two more
+// K-float arrays per thread (the quad's sum and the Kahan correction).
+template <int K, bool COMP>
+constexpr int min_blocks() {
+  return COMP ? (K >= 16 ? 2 : 4) : (K >= 16 ? kMinBlocks16 : kMinBlocks);
+}
+
+// COMP: compensated summation - each quad's (four angles') products are an
+// FMA chain added to the pixel's sum with Kahan's correction.
+template <int K, int LK, bool EXACT, bool PEN, bool FH, bool COMP>
+__global__ void __launch_bounds__(kBlock, (min_blocks<K, COMP>()))
     k_backward(IterArgs A, int batch, const float* __restrict__ cur,
                float* __restrict__ next, const float* __restrict__ upd,
                float* __restrict__ rep_num, int epi) {
@@ -186,9 +195,9 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
 #pragma unroll
     for (int j = 0; j < K; ++j) rf[j] = v.v[j];
   }
-  float acc[K];
+  float acc[K], cmp[K];
 #pragma unroll
-  for (int j = 0; j < K; ++j) acc[j] = 0.f;
+  for (int j = 0; j < K; ++j) acc[j] = cmp[j] = 0.f;
   // the fixed-point scale of 16-bit codes is applied once, at the end
   // (half factors take the scaled length: it is rounded to a half)
   constexpr bool kScaled = (LK == LK_U16) && !EXACT && !FH;
@@ -211,6 +220,8 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
     for (int a4 = 0; a4 < na; a4 += 4) {
       Quad<LK> nq;
       if (a4 + 4 < na) load_quad<LK>(qp + qstep, nq);
+      // the quad's four angles into t
+      auto quad_body = [&](float (&t)[K]) {
       if constexpr (FH && !EXACT && K >= 2 && K <= 8) {
         // software pipeline over the quad's 4 angles: the factor loads of
         // angle j + 1 are in flight while angle j's FMAs run
@@ -240,10 +251,10 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
           for (int i = 0; i < K / 2; ++i) {
             asm("{ .reg .b16 lo, hi, l0, l1; mov.b32 {lo, hi}, %2; mov.b32 {l0, l1}, %3;"
                 " fma.rn.f32.f16 %0, lo, l0, %0; fma.rn.f32.f16 %1, hi, l0, %1; }"
-                : "+f"(acc[2 * i]), "+f"(acc[2 * i + 1]) : "r"(w0[b][i]), "r"(lw[b]));
+                : "+f"(t[2 * i]), "+f"(t[2 * i + 1]) : "r"(w0[b][i]), "r"(lw[b]));
             asm("{ .reg .b16 lo, hi, l0, l1; mov.b32 {lo, hi}, %2; mov.b32 {l0, l1}, %3;"
                 " fma.rn.f32.f16 %0, lo, l1, %0; fma.rn.f32.f16 %1, hi, l1, %1; }"
-                : "+f"(acc[2 * i]), "+f"(acc[2 * i + 1]) : "r"(w1[b][i]), "r"(lw[b]));
+                : "+f"(t[2 * i]), "+f"(t[2 * i + 1]) : "r"(w1[b][i]), "r"(lw[b]));
           }
         };
         issue(0, 0);
@@ -252,7 +263,7 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
           if (j < 3) issue(j + 1, (j + 1) & 1);
           consume(j & 1);
         }
-      } else
+      } else {
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         float l0, l1;
@@ -267,9 +278,21 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
           const float* ub1 = FH ? reinterpret_cast<const float*>(
                                       reinterpret_cast<const __half*>(ub) + K)
                                 : ub + K;
-          if (h0) accumulate<K, EXACT, PEN, FH>(acc, rf, l0, ub);
-          if (h1) accumulate<K, EXACT, PEN, FH>(acc, rf, l1, ub1);
+          if (h0) accumulate<K, EXACT, PEN, FH>(t, rf, l0, ub);
+          if (h1) accumulate<K, EXACT, PEN, FH>(t, rf, l1, ub1);
         }
+      }
+      }
+      };
+      if constexpr (COMP) {
+        float qa[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) qa[j] = 0.f;
+        quad_body(qa);
+#pragma unroll
+        for (int j = 0; j < K; ++j) kahan_add(acc[j], cmp[j], qa[j]);
+      } else {
+        quad_body(acc);
       }
       q = nq;
       qp += qstep;
@@ -278,6 +301,10 @@ __global__ void __launch_bounds__(kBlock, K >= 16 ? kMinBlocks16 : kMinBlocks)
     }
   }
   if (!valid) return;
+  if constexpr (COMP) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) acc[j] = fsub(acc[j], cmp[j]);
+  }
   // with half factors the lengths are taken as halves: their own total
   const float Wp = FH ? A.M.Wh[p] : A.M.W[p];
   if constexpr (kScaled) {
@@ -337,14 +364,21 @@ void back_launch(const IterArgs& A, int batch, const float* cur, float* next,
                  const float* upd, float* rep_num, int epi, cudaStream_t st) {
   const int blocks = (A.M.ntiles + kWarps - 1) / kWarps;
   const bool pen = A.alg >= 2;
-#define TG_BACK(E, PN, FH) \
-  k_backward<K, LK, E, PN, FH><<<blocks, kBlock, 0, st>>>(A, batch, cur, next, upd, rep_num, epi)
+#define TG_BACK(E, PN, FH, CP)                                                        \
+  k_backward<K, LK, E, PN, FH, CP><<<blocks, kBlock, 0, st>>>(A, batch, cur, next, upd, \
+                                                             rep_num, epi)
   if (A.exact) {
-    if (pen) TG_BACK(true, true, false); else TG_BACK(true, false, false);
+    if (pen) TG_BACK(true, true, false, false); else TG_BACK(true, false, false, false);
+  } else if (A.comp) {
+    if (A.half_factors) {
+      if (pen) TG_BACK(false, true, true, true); else TG_BACK(false, false, true, true);
+    } else {
+      if (pen) TG_BACK(false, true, false, true); else TG_BACK(false, false, false, true);
+    }
   } else if (A.half_factors) {
-    if (pen) TG_BACK(false, true, true); else TG_BACK(false, false, true);
+    if (pen) TG_BACK(false, true, true, false); else TG_BACK(false, false, true, false);
   } else {
-    if (pen) TG_BACK(false, true, false); else TG_BACK(false, false, false);
+    if (pen) TG_BACK(false, true, false, false); else TG_BACK(false, false, false, false);
   }
 #undef TG_BACK
 }

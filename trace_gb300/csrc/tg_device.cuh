@@ -16,6 +16,15 @@ namespace tg {
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+
+// Kahan's compensated summation: s += x, with c carrying the low-order part
+// the rounded additions lost (s - c is the corrected sum).
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = fsub(x, c);
+  const float t = fadd(s, y);
+  c = fsub(fsub(t, s), y);
+  s = t;
+}
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
 
@@ -294,6 +303,29 @@ __device__ __forceinline__ void store_vec(float* p, const Vec<K>& r) {
       *reinterpret_cast<float4*>(p + j) =
           make_float4(r.v[j], r.v[j + 1], r.v[j + 2], r.v[j + 3]);
   }
+}
+
+// K floats read once (streaming loads: evict-first).
+template <int K>
+__device__ __forceinline__ Vec<K> load_vec_cs(const float* p) {
+  Vec<K> r;
+  if constexpr (K == 1) {
+    r.v[0] = __ldcs(p);
+  } else if constexpr (K == 2) {
+    const float2 t = __ldcs(reinterpret_cast<const float2*>(p));
+    r.v[0] = t.x;
+    r.v[1] = t.y;
+  } else {
+#pragma unroll
+    for (int j = 0; j < K; j += 4) {
+      const float4 t = __ldcs(reinterpret_cast<const float4*>(p + j));
+      r.v[j] = t.x;
+      r.v[j + 1] = t.y;
+      r.v[j + 2] = t.z;
+      r.v[j + 3] = t.w;
+    }
+  }
+  return r;
 }
 
 // acc[j] += l * v[j] for the K slices (fast mode). Scalar FMAs: the paired

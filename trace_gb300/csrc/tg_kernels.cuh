@@ -60,10 +60,19 @@ __device__ __forceinline__ bool unit_step(int ix, int iy, int px, int py) {
   const int dx = ix - px, dy = iy - py;
   return dx >= 0 && dx <= 1 && dy >= -1 && dy <= 1;
 }
+// Each run's partial sums (K floats) go to a slot fixed at construction:
+// rays are taken in groups of 32 (ray r in group r / 32 at lane r % 32), and
+// run k of ray r (k-th in the order its path crosses the tiles) has slot
+// pbase[r / 32] + k * 32 + r % 32, so the finish kernel's warp reads one
+// contiguous row of 32 slots per run ordinal while each lane adds its ray's
+// runs in path order. No atomics: the forward projection is bit-reproducible.
 struct TileMatrixDev {
   int tiles_x, ntiles;
   const int* group_first;   // [ntiles + 1] first group of each tile
-  const int* gray;          // [groups * 32] ray of each lane, -1 if empty
+  const int* gpart;         // [groups * 32] partial-sum slot of each lane's
+                            // run, -1 if the lane is empty
+  const int* rnrun;         // [P*C] runs of each ray
+  const int* pbase;         // [ceil(P*C / 32)] first slot of each ray group
   const uint16_t* glp;      // [groups * 32] first pixel, tile-local (y*64 + x)
   const uint16_t* glen;     // [groups * 32] run length (segments)
   const int* gsteps;        // [groups] longest run of the group
@@ -100,6 +109,9 @@ struct IterArgs {
   //             backprojection adds the per-pixel total length back
   int half_tile;
   int half_factors;
+  // compensated (Kahan) summation of the ray and pixel sums (fast mode,
+  // tile-staged forward, L1 backprojection)
+  int comp;
 };
 
 // Address of (slot, pixel) in the batched reconstruction layout.
@@ -204,17 +216,20 @@ int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
 void launch_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
                        int64_t nruns, const int* tile_first_run,
                        const int* group_first, const uint16_t* run_lp,
-                       const uint16_t* run_len, int* gray, uint16_t* glp,
+                       const uint16_t* run_len, const int64_t* ray_run_off,
+                       const int* pbase, int* gpart, uint16_t* glp,
                        uint16_t* glen, int* gsteps, int* run_slot,
                        cudaStream_t st);
 void launch_runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x,
                       const int64_t* ray_run_off, const int* run_slot,
                       const int64_t* gseg_off, const int64_t* gcode_off,
                       void* tlen, uint32_t* tcode, cudaStream_t st);
+// part: [runs][K] partial sums, written (not accumulated) by each launch
 void launch_forward_tiled(const IterArgs& A, const TileMatrixDev& T,
-                          const float* recon_batch, float* sim, cudaStream_t st);
-void launch_fwd_finish(const IterArgs& A, float* sim, const float* sino,
-                       float* out, int out_mode, cudaStream_t st);
+                          const float* recon_batch, float* part, cudaStream_t st);
+// ray sums from the partial sums (fixed order) -> per-ray values `out`
+void launch_fwd_finish(const IterArgs& A, const TileMatrixDev& T, const float* part,
+                       const float* sino, float* out, int out_mode, cudaStream_t st);
 // tg_iter.cu
 void launch_fg(const IterArgs& A, const float* recon, const float* W, float* F,
                float* Gv, cudaStream_t st);

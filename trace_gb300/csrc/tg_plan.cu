@@ -5,7 +5,6 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -38,10 +37,11 @@ struct tg_plan {
   float* d_Wh = nullptr;  // half_gathers: total of the half-rounded lengths
   int* d_exc_first = nullptr;  // window exceptions (CSR over 8x4 tiles)
   int4* d_exc = nullptr;
-  // tile-staged forward (fast mode): the tile-ordered matrix + ray sums
+  // tile-staged forward (fast mode): the tile-ordered matrix + the runs'
+  // partial sums ([runs][K], one slot per run)
   bool tiles = false;
   TileMatrixDev T{};
-  float* d_sim = nullptr;
+  float* d_part = nullptr;
   // FP64 mode: double state, factors, total lengths and SIRT's a2
   bool fp64 = false;
   double *d_ra2d = nullptr, *d_W64 = nullptr;
@@ -50,6 +50,10 @@ struct tg_plan {
   float* d_sino = nullptr;
   float* d_recon[2] = {nullptr, nullptr};
   int cur = 0;
+  // fused iterations since the reconstruction was last reset or uploaded:
+  // with half_gathers the first one keeps FP32 factors (factors start far
+  // from 1, where a half of factor - 1 loses the most)
+  int64_t iters_done = 0;
   float* d_upd = nullptr;
   float* d_rep = nullptr;
   float *d_F = nullptr, *d_G = nullptr;
@@ -72,9 +76,14 @@ struct tg_plan {
   struct Graph {
     bool valid = false;
     int alg = -1;
+    int half_factors = -1;
     tg_params prm{};
     cudaGraphExec_t exec = nullptr;
   } graphs[2];
+  // device address of the allocation-free entry point's factor array in the
+  // context this plan was created in (looked up at creation), or nullptr
+  float* noalloc_factors = nullptr;
+  std::string noalloc_err;
   // per-kernel timers: event pairs recorded around launches while enabled
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -198,6 +207,7 @@ IterArgs make_args(tg_plan* p, int alg, const tg_params* prm) {
   A.nslots = p->nslots;
   A.slice_id = p->d.slice_id;
   A.num_total_slices = p->d.num_total_slices;
+  A.comp = p->d.compensated;
   fill_weights(p, prm, A.pw);
   return A;
 }
@@ -254,6 +264,7 @@ int establish_layout(tg_plan* p, int alg) {
   p->nslots = nslots;
   p->layout_alg = alg;
   p->cur = 0;
+  p->iters_done = 0;
   return TG_OK;
 }
 
@@ -349,19 +360,38 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
   }
   tile_first[ntiles] = runs;
   group_first[ntiles] = groups;
-  int *d_tile_first, *d_group_first, *gray, *gsteps;
+  // partial-sum slots: per group of 32 rays, one row of 32 slots per run
+  // ordinal up to the group's longest run count
+  const int64_t rgroups = (p->R + 31) / 32;
+  std::vector<int> pbase_h(rgroups);
+  int64_t nslots = 0;
+  for (int64_t gi = 0; gi < rgroups; ++gi) {
+    int most = 0;
+    for (int64_t r = gi * 32; r < std::min<int64_t>(p->R, gi * 32 + 32); ++r)
+      most = std::max(most, nruns[r]);
+    pbase_h[gi] = (int)nslots;
+    nslots += (int64_t)most * 32;
+    if (nslots > 0x7fffffff)
+      return release(), fail(p, TG_E_GEOMETRY, "too many partial-sum slots");
+  }
+  int *d_tile_first, *d_group_first, *gpart, *gsteps, *rnrun, *pbase;
   uint16_t *glp, *glen;
   if ((rc = talloc(&d_tile_first, (size_t)ntiles + 1, false)) ||
       (rc = dalloc(p, &d_group_first, (size_t)ntiles + 1)) ||
-      (rc = dalloc(p, &gray, (size_t)groups * 32)) ||
+      (rc = dalloc(p, &gpart, (size_t)groups * 32)) ||
+      (rc = dalloc(p, &rnrun, (size_t)p->R)) ||
+      (rc = dalloc(p, &pbase, (size_t)rgroups)) ||
       (rc = dalloc(p, &glp, (size_t)groups * 32, true)) ||
       (rc = dalloc(p, &glen, (size_t)groups * 32, true)) ||
       (rc = dalloc(p, &gsteps, (size_t)groups, true)))
     return release(), rc;
-  cudaMemsetAsync(gray, 0xff, (size_t)groups * 32 * 4, p->st);  // empty lanes: -1
+  cudaMemsetAsync(gpart, 0xff, (size_t)groups * 32 * 4, p->st);  // empty lanes: -1
   cudaMemcpyAsync(d_tile_first, tile_first.data(), (ntiles + 1) * 4, cudaMemcpyHostToDevice, p->st);
   cudaMemcpyAsync(d_group_first, group_first.data(), (ntiles + 1) * 4, cudaMemcpyHostToDevice, p->st);
-  launch_runs_group(rk, key2, val2, NR, d_tile_first, d_group_first, run_lp, run_len, gray,
+  cudaMemcpyAsync(rnrun, nruns.data(), p->R * 4, cudaMemcpyHostToDevice, p->st);
+  cudaMemcpyAsync(pbase, pbase_h.data(), rgroups * 4, cudaMemcpyHostToDevice, p->st);
+  launch_runs_group(rk, key2, val2, NR, d_tile_first, d_group_first, run_lp, run_len,
+                    d_run_off, pbase, gpart,
                     glp, glen, gsteps, run_slot, p->st);
   std::vector<int> steps(groups);
   cudaMemcpyAsync(steps.data(), gsteps, (size_t)groups * 4, cudaMemcpyDeviceToHost, p->st);
@@ -397,12 +427,14 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
                    tcode, p->st);
   if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run fill failed");
   release();
-  if ((rc = dalloc(p, &p->d_sim, (size_t)p->R * p->K, true))) return rc;
+  if ((rc = dalloc(p, &p->d_part, (size_t)nslots * p->K))) return rc;
   TileMatrixDev& T = p->T;
   T.tiles_x = tiles_x;
   T.ntiles = ntiles;
   T.group_first = d_group_first;
-  T.gray = gray;
+  T.gpart = gpart;
+  T.rnrun = rnrun;
+  T.pbase = pbase;
   T.glp = glp;
   T.glen = glen;
   T.gsteps = gsteps;
@@ -412,6 +444,7 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
   T.tcode = tcode;
   p->tiles = true;
   p->info.tile_runs = NR;
+  p->info.partial_slots = nslots;
   p->info.tile_bytes = entries * (l16 ? 2 : 4) + words * 4 + (int64_t)groups * (32 * 8 + 20);
   return TG_OK;
 }
@@ -432,6 +465,9 @@ int fp32_only(tg_plan* p) {
 double* as_f64(float* p) { return reinterpret_cast<double*>(p); }
 
 }  // namespace
+
+// tg_reduce_slice_noalloc's factor array, looked up for each new plan
+static void resolve_noalloc_factors(tg_plan* p);
 
 extern "C" {
 
@@ -477,6 +513,9 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
       (d.len_storage != TG_LEN_F32 || d.slices_per_pass != 1 || d.delta_index))
     return fail(nullptr, TG_E_ARG,
                 "FP64 mode needs f32 lengths, explicit indices and one slice per pass");
+  if (d.compensated && (d.mode != TG_MODE_FAST || !d.forward_tiles || d.backward_staged))
+    return fail(nullptr, TG_E_ARG,
+                "compensated needs fast mode, forward_tiles and the L1 backprojection");
   if ((sin_tab == nullptr) != (cos_tab == nullptr))
     return fail(nullptr, TG_E_ARG, "give both sin_tab and cos_tab or neither");
 
@@ -780,6 +819,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   I.backward_bytes = (int64_t)dense_n * (int64_t)lbytes;
   I.max_segment_length = maxlen;
   I.setup_ms = ms;
+  resolve_noalloc_factors(p);
   *out = p;
   return TG_OK;
 }
@@ -949,8 +989,9 @@ int tg_get_recon(tg_plan* p, int alg, float* recon, int on_device) {
 }
 
 // Forward projection of batch b into per-ray values `out` (FP32): the
-// tile-ordered kernel (ray sums by atomics, plus the finish kernel) when the
-// plan has the tile-ordered matrix, else the ray-ordered kernel.
+// tile-ordered kernel (per-run partial sums, added per ray in path order by
+// the finish kernel) when the plan has the tile-ordered matrix, else the
+// ray-ordered kernel.
 static int run_forward(tg_plan* p, const IterArgs& A0, int b, int out_mode,
                        float* out) {
   const float* src = batch_ptr(p, p->d_recon[p->cur], b * p->K + p->fshift);
@@ -960,11 +1001,12 @@ static int run_forward(tg_plan* p, const IterArgs& A0, int b, int out_mode,
     A.half_factors = 0;
     {
       Timed t(p, 0);
-      launch_forward_tiled(A, p->T, src, p->d_sim, p->st);
+      launch_forward_tiled(A, p->T, src, p->d_part, p->st);
     }
     Timed t(p, 2);
-    launch_fwd_finish(A, p->d_sim, p->d_sino ? p->d_sino + (int64_t)b * p->R * p->K : nullptr,
-                      out, out_mode, p->st);
+    launch_fwd_finish(A, p->T, p->d_part,
+                      p->d_sino ? p->d_sino + (int64_t)b * p->R * p->K : nullptr, out,
+                      out_mode, p->st);
     return TG_OK;
   }
   const IterArgs& A = A0;
@@ -974,23 +1016,29 @@ static int run_forward(tg_plan* p, const IterArgs& A0, int b, int out_mode,
   return TG_OK;
 }
 
+// Whether this plan's next fused iteration stores its ratio factors as
+// halves of (factor - 1): half_gathers plans from their second iteration on.
+static int half_factors_next(const tg_plan* p, int mode) {
+  return p->tiles && p->d.half_gathers && mode == FWD_RATIO && p->iters_done >= 1;
+}
+
 // Launches of one fused iteration on the plan's stream (buffers by p->cur;
-// the caller flips p->cur).
+// the caller flips p->cur and counts the iteration).
 static void issue_iteration(tg_plan* p, const IterArgs& A0, int mode) {
   IterArgs A = A0;
   if (p->tiles && p->d.half_gathers) {
     A.half_tile = 1;
-    A.half_factors = mode == FWD_RATIO;
+    A.half_factors = half_factors_next(p, mode);
   }
   for (int b = 0; b < p->nb; ++b) {
     if (p->tiles) {
       const float* src = batch_ptr(p, p->d_recon[p->cur], b * p->K + p->fshift);
       {
         Timed t(p, 0);
-        launch_forward_tiled(A, p->T, src, p->d_sim, p->st);
+        launch_forward_tiled(A, p->T, src, p->d_part, p->st);
       }
       Timed t(p, 2);
-      launch_fwd_finish(A, p->d_sim, p->d_sino + (int64_t)b * p->R * p->K,
+      launch_fwd_finish(A, p->T, p->d_part, p->d_sino + (int64_t)b * p->R * p->K,
                         p->d_upd, mode, p->st);
     } else {
       run_forward(p, A, b, mode, p->d_upd);
@@ -1055,7 +1103,8 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
   for (int it = 0; it < n_iter; ++it) {
     if (graphs) {
       tg_plan::Graph& g = p->graphs[p->cur];
-      if (!g.valid || g.alg != alg || !same_params(g.prm, prm)) {
+      const int hf = half_factors_next(p, mode);
+      if (!g.valid || g.alg != alg || g.half_factors != hf || !same_params(g.prm, prm)) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g = tg_plan::Graph();
         cudaGraph_t graph;
@@ -1067,6 +1116,7 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
         if (e != cudaSuccess) return fail(p, TG_E_CUDA, cudaGetErrorString(e));
         g.valid = true;
         g.alg = alg;
+        g.half_factors = hf;
         g.prm = prm ? *prm : tg_params{};
       }
       TG_CUDA(p, cudaGraphLaunch(g.exec, p->st));
@@ -1074,6 +1124,7 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
       issue_iteration(p, A, mode);
     }
     p->cur ^= 1;
+    ++p->iters_done;
   }
   TG_CUDA(p, cudaGetLastError());
   return TG_OK;
@@ -1089,6 +1140,7 @@ struct tg_batch {
   struct Graph {
     bool valid = false;
     std::vector<int> algs;
+    std::vector<int> half_factors;  // per plan, as issue_iteration decides
     std::vector<tg_params> prms;
     int cur0 = -1;  // plan 0's buffer parity the graph was captured in
     cudaGraphExec_t exec = nullptr;
@@ -1175,7 +1227,10 @@ extern "C" int tg_batch_iterate(tg_batch* b, const int* algs, const tg_params* p
   for (int it = 0; it < n_iter; ++it) {
     const int parity = b->plans[0]->cur;
     tg_batch::Graph& g = b->graphs[parity];
-    bool match = g.valid && g.cur0 == parity;
+    std::vector<int> hf(n);
+    for (int i = 0; i < n; ++i)
+      hf[i] = half_factors_next(b->plans[i], algs[i] == TG_SIRT ? FWD_SIRT : FWD_RATIO);
+    bool match = g.valid && g.cur0 == parity && g.half_factors == hf;
     for (int i = 0; match && i < n; ++i)
       match = g.algs[i] == algs[i] &&
               same_params(g.prms[i], params ? &params[i] : nullptr);
@@ -1212,6 +1267,7 @@ extern "C" int tg_batch_iterate(tg_batch* b, const int* algs, const tg_params* p
       }
       g.valid = true;
       g.cur0 = parity;
+      g.half_factors = hf;
       g.algs.assign(algs, algs + n);
       for (int i = 0; i < n; ++i) g.prms.push_back(params ? params[i] : tg_params{});
     }
@@ -1220,7 +1276,10 @@ extern "C" int tg_batch_iterate(tg_batch* b, const int* algs, const tg_params* p
       b->err = cudaGetErrorString(e);
       return TG_E_CUDA;
     }
-    for (tg_plan* p : b->plans) p->cur ^= 1;
+    for (tg_plan* p : b->plans) {
+      p->cur ^= 1;
+      ++p->iters_done;
+    }
   }
   // later calls on the plans' own streams see the batch's results
   const cudaError_t e = cudaStreamSynchronize(b->main);
@@ -1387,32 +1446,24 @@ namespace {
 constexpr int64_t kNoAllocMaxRays = int64_t(1) << 22;  // 4,194,304 floats
 static __device__ __align__(256) float g_noalloc_factors[kNoAllocMaxRays];
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-float* g_noalloc_addr[kNoAllocMaxDevices] = {};
-
-// Device address of the array on the current device, looked up once per
-// device. In host code the array's name is only a host-side stand-in.
-int noalloc_factors(tg_plan* p, float** out) {
-  int dev = -1;
-  TG_CUDA(p, cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kNoAllocMaxDevices)
-    return fail(p, TG_E_LIMIT, "device ordinal outside 0..63");
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
-    void* addr = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_factors);
-    if (e != cudaSuccess || !addr)
-      return fail(p, TG_E_CUDA,
-                  std::string("cudaGetSymbolAddress of the factor array: ") +
-                      cudaGetErrorString(e));
-    g_noalloc_addr[dev] = static_cast<float*>(addr);
-  }
-  *out = g_noalloc_addr[dev];
-  return TG_OK;
-}
-
 }  // namespace
+
+// Device address of the array in the current context, stored in the plan at
+// its creation (the plan's device is current then; in host code the array's
+// name is only a host-side stand-in, never a device address). A plan lives
+// in one context, so the address cannot go stale under it; looking it up
+// here also loads the array on the device before any allocation-free call.
+static void resolve_noalloc_factors(tg_plan* p) {
+  void* addr = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_factors);
+  if (e != cudaSuccess || !addr) {
+    cudaGetLastError();
+    p->noalloc_err = std::string("cudaGetSymbolAddress of the factor array: ") +
+                     cudaGetErrorString(e);
+    return;
+  }
+  p->noalloc_factors = static_cast<float*>(addr);
+}
 
 extern "C" int tg_reduce_slice_noalloc(tg_plan* p, int alg,
                                        const tg_params* prm, const float* recon,
@@ -1426,8 +1477,8 @@ extern "C" int tg_reduce_slice_noalloc(tg_plan* p, int alg,
                 "P*C = " + std::to_string(p->R) +
                     " rays exceeds the 4,194,304-ray factor array of "
                     "tg_reduce_slice_noalloc");
-  float* factors = nullptr;
-  TG_TRY(noalloc_factors(p, &factors));
+  if (!p->noalloc_factors) return fail(p, TG_E_CUDA, p->noalloc_err);
+  float* factors = p->noalloc_factors;
   IterArgs A = make_args(p, alg, prm);
   A.K = 1;  // one slice: plain [C*C] / [P*C] layouts
   A.S = 1;

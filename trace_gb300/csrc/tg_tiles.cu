@@ -11,11 +11,13 @@
 // 8 segments for 16-bit codes) with 8 bytes of step deltas per chunk,
 // chunks interleaved across the 32 lanes so each chunk load of a warp is one
 // contiguous 512-byte row; the next chunk is loaded while the current one is
-// consumed. A run's partial sum is added to its ray's sum with
-// one vector reduction; tg::launch_fwd_finish turns the sums into the
-// per-ray factors the backprojection reads and clears them for the next
-// batch. Summation order across runs is not fixed, so this path is used in
-// fast mode only.
+// consumed. A run's partial sums (K floats, FMA chain in step order) are
+// stored, not accumulated, into the run's own slot (TileMatrixDev: slot of
+// run k of ray r = pbase[r / 32] + 32 k + r % 32). tg::launch_fwd_finish adds
+// a ray's slots in path order and turns the sums into the per-ray factors
+// the backprojection reads. No atomics anywhere, so every launch gives the same
+// bits; the sum is the reference's sequential ray sum (sirt.cc:10-17)
+// regrouped by tile runs, which is why this path is fast mode only.
 //
 // Construction (once per geometry): runs per ray are counted by the tracing
 // pass that counts segments (k_trace_count); then run records keyed by
@@ -148,7 +150,8 @@ __global__ void __launch_bounds__(kTraceBlock)
 __global__ void k_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
                              int64_t nruns, const int* tile_first_run,
                              const int* group_first, const uint16_t* run_lp,
-                             const uint16_t* run_len, int* gray, uint16_t* glp,
+                             const uint16_t* run_len, const int64_t* ray_run_off,
+                             const int* pbase, int* gpart, uint16_t* glp,
                              uint16_t* glen, int* gsteps, int* run_slot) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nruns) return;
@@ -157,9 +160,14 @@ __global__ void k_runs_group(RunKey rk, const unsigned long long* skey, const in
   const int rank = (int)(j - tile_first_run[t]);
   const int grp = group_first[t] + rank / 32;
   const int lane = rank % 32;
+  // i: the run's index in emission order (k_runs_emit numbers ray r's runs
+  // ray_run_off[r], ray_run_off[r] + 1, ... along the ray), so its ordinal
+  // on the ray is i - ray_run_off[r]
   const int i = sval[j];
   const int slot = grp * 32 + lane;
-  gray[slot] = (int)((k >> 8) & ((1ull << rk.ray_bits) - 1));
+  const int64_t r = (int64_t)((k >> 8) & ((1ull << rk.ray_bits) - 1));
+  const int ord = (int)(i - ray_run_off[r]);
+  gpart[slot] = pbase[r >> 5] + ord * 32 + (int)(r & 31);
   glp[slot] = run_lp[i];
   glen[slot] = run_len[i];
   run_slot[i] = slot;
@@ -327,22 +335,19 @@ __device__ __forceinline__ void tile_fma(const float* sm, int si, float l,
   }
 }
 
+// A run's K partial sums into its slot (streaming stores: the finish kernel
+// reads each slot once).
 template <int K>
-__device__ __forceinline__ void red_add(float* dst, const float (&acc)[K]) {
+__device__ __forceinline__ void store_part(float* dst, const float (&acc)[K]) {
+  if constexpr (K >= 4) {
 #pragma unroll
-  for (int j = 0; j < K; j += 4) {
-    if constexpr (K >= 4) {
-      asm volatile("red.global.add.v4.f32 [%0], {%1,%2,%3,%4};" ::"l"(dst + j),
-                   "f"(acc[j]), "f"(acc[j + 1]), "f"(acc[j + 2]), "f"(acc[j + 3])
-                   : "memory");
-    }
-  }
-  if constexpr (K == 2) {
-    asm volatile("red.global.add.v2.f32 [%0], {%1,%2};" ::"l"(dst), "f"(acc[0]),
-                 "f"(acc[1])
-                 : "memory");
-  } else if constexpr (K == 1) {
-    atomicAdd(dst, acc[0]);
+    for (int j = 0; j < K; j += 4)
+      __stcs(reinterpret_cast<float4*>(dst + j),
+             make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]));
+  } else if constexpr (K == 2) {
+    __stcs(reinterpret_cast<float2*>(dst), make_float2(acc[0], acc[1]));
+  } else {
+    __stcs(dst, acc[0]);
   }
 }
 
@@ -385,16 +390,19 @@ __device__ __forceinline__ float chunk_len(const Chunk<LK>& ch, int j,
   }
 }
 
-template <int K, int LK, bool H>
+// COMP: compensated summation - each chunk's 8 products are an FMA chain
+// added to the run's sum with Kahan's correction (the stored partial sum is
+// the corrected one).
+template <int K, int LK, bool H, bool COMP>
 __global__ void __launch_bounds__(kBlock)
     k_forward_tiled(TileMatrixDev T, int g, float inv_scale, int splits,
-                    const float* __restrict__ recon, float* __restrict__ sim) {
+                    const float* __restrict__ recon, float* __restrict__ part) {
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   __half* smh = reinterpret_cast<__half*>(smem4);
   // `splits` blocks share a tile (small grids: fewer tiles than SMs); each
   // loads the tile and takes every splits-th warp group
-  const int t = blockIdx.x / splits, part = blockIdx.x - t * splits;
+  const int t = blockIdx.x / splits, sub = blockIdx.x - t * splits;
   const int x0 = (t % T.tiles_x) * TS, y0 = (t / T.tiles_x) * TS;
   if constexpr (H)
     tile_load_half<K>(smh, recon, g, x0, y0);
@@ -403,22 +411,21 @@ __global__ void __launch_bounds__(kBlock)
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g0 = T.group_first[t], g1 = T.group_first[t + 1];
-  for (int grp = g0 + part * (kBlock / 32) + warp; grp < g1; grp += splits * (kBlock / 32)) {
+  for (int grp = g0 + sub * (kBlock / 32) + warp; grp < g1; grp += splits * (kBlock / 32)) {
     const int slot = grp * 32 + lane;
-    const int ray = T.gray[slot];
-    const int n = T.glen[slot];
+    const int pslot = T.gpart[slot];
     const int lp = T.glp[slot];
     int si = (lp / TS) * RS + lp % TS;  // shared-memory index of the current pixel
     const int chunks = (T.gsteps[grp] + 7) >> 3;
     const int64_t lb = T.gseg_off[grp] + lane * 8;
     const int64_t cb = T.gcode_off[grp] + lane * 2;
-    float acc[K];
+    float acc[K], cmp[K];
 #pragma unroll
-    for (int j = 0; j < K; ++j) acc[j] = 0.f;
+    for (int j = 0; j < K; ++j) acc[j] = cmp[j] = 0.f;
     Chunk<LK> cur, nxt;
     if (chunks > 0) load_chunk<LK>(T, lb, cb, 0, cur);
-    for (int c = 0; c < chunks; ++c) {
-      if (c + 1 < chunks) load_chunk<LK>(T, lb, cb, c + 1, nxt);
+    // one chunk's 8 steps into a
+    auto chunk_steps = [&](float (&a)[K]) {
       // No per-step guard: a run's first step and every step past its end
       // carry the "stay" step 0 and a zero length (see k_runs_fill), so
       // lanes of shorter runs add 0 * (a finite pixel value) in place.
@@ -426,31 +433,68 @@ __global__ void __launch_bounds__(kBlock)
       for (int j = 0; j < 8; ++j) {
         si += (int)(int8_t)((j < 4 ? cur.code.x : cur.code.y) >> (8 * (j & 3)));
         if constexpr (H)
-          tile_fma_half<K>(smh, si, chunk_len<LK>(cur, j, inv_scale), acc);
+          tile_fma_half<K>(smh, si, chunk_len<LK>(cur, j, inv_scale), a);
         else
-          tile_fma<K>(sm, si, chunk_len<LK>(cur, j, inv_scale), acc);
+          tile_fma<K>(sm, si, chunk_len<LK>(cur, j, inv_scale), a);
+      }
+    };
+    for (int c = 0; c < chunks; ++c) {
+      if (c + 1 < chunks) load_chunk<LK>(T, lb, cb, c + 1, nxt);
+      if constexpr (COMP) {
+        float ca[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) ca[j] = 0.f;
+        chunk_steps(ca);
+#pragma unroll
+        for (int j = 0; j < K; ++j) kahan_add(acc[j], cmp[j], ca[j]);
+      } else {
+        chunk_steps(acc);
       }
       cur = nxt;
+    }
+    if constexpr (COMP) {
+#pragma unroll
+      for (int j = 0; j < K; ++j) acc[j] = fsub(acc[j], cmp[j]);
     }
     if constexpr (LK == LK_U16) {
 #pragma unroll
       for (int j = 0; j < K; ++j) acc[j] *= inv_scale;
     }
-    if (ray >= 0 && n > 0) red_add<K>(sim + (int64_t)ray * K, acc);
+    if (pslot >= 0) store_part<K>(part + (int64_t)pslot * K, acc);
   }
 }
 
-// sums -> per-ray factor (as k_forward's epilogue), then clear the sums.
-// FH (ratio factors only): the factor is stored as the half (ray/sim - 1).
-template <int K, bool FH>
-__global__ void k_fwd_finish(int64_t nrays, const float* __restrict__ ra2,
-                             float* __restrict__ sim, const float* __restrict__ sino,
+// A ray's partial sums (its runs' slots, in path order) -> per-ray factor,
+// as k_forward's epilogue. FH (ratio factors only): the factor is stored as
+// the half (ray/sim - 1).
+template <int K, bool FH, bool COMP>
+__global__ void k_fwd_finish(int64_t nrays, const int* __restrict__ rnrun,
+                             const int* __restrict__ pbase,
+                             const float* __restrict__ ra2,
+                             const float* __restrict__ part,
+                             const float* __restrict__ sino,
                              float* __restrict__ out, int out_mode) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrays) return;
   Vec<K> s;
+  float cmp[K];
 #pragma unroll
-  for (int j = 0; j < K; ++j) s.v[j] = sim[r * K + j];
+  for (int j = 0; j < K; ++j) s.v[j] = cmp[j] = 0.f;
+  const int n = rnrun[r];
+  // the warp's 32 rays are one ray group: run k of every lane is one row
+  const float* src = part + ((int64_t)pbase[r >> 5] + (r & 31)) * K;
+  for (int k = 0; k < n; ++k) {
+    const Vec<K> v = load_vec_cs<K>(src + (int64_t)k * 32 * K);
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if constexpr (COMP) kahan_add(s.v[j], cmp[j], v.v[j]);
+      else s.v[j] = fadd(s.v[j], v.v[j]);
+    }
+  }
+  if constexpr (COMP) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) s.v[j] = fsub(s.v[j], cmp[j]);
+  }
   Vec<K> o;
   if (out_mode == FWD_SIM) {
     o = s;
@@ -469,50 +513,50 @@ __global__ void k_fwd_finish(int64_t nrays, const float* __restrict__ ra2,
   } else {
     store_vec<K>(out + r * K, o);
   }
-  Vec<K> z;
-#pragma unroll
-  for (int j = 0; j < K; ++j) z.v[j] = 0.f;
-  store_vec<K>(sim + r * K, z);
 }
 
-template <int K, int LK, bool H>
+template <int K, int LK, bool H, bool COMP>
 void fwd_tiled_launch(const TileMatrixDev& T, int g, float inv_scale,
-                      const float* recon, float* sim, cudaStream_t st) {
+                      const float* recon, float* part, cudaStream_t st) {
   const int smem = TilePlanes<K, H>::kBytes;
-  cudaFuncSetAttribute(k_forward_tiled<K, LK, H>,
+  cudaFuncSetAttribute(k_forward_tiled<K, LK, H, COMP>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   // at least two blocks per SM when the grid has few tiles
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int splits = max(1, min(16, (2 * sms + T.ntiles - 1) / T.ntiles));
-  k_forward_tiled<K, LK, H><<<T.ntiles * splits, kBlock, smem, st>>>(T, g, inv_scale, splits,
-                                                                     recon, sim);
+  k_forward_tiled<K, LK, H, COMP><<<T.ntiles * splits, kBlock, smem, st>>>(
+      T, g, inv_scale, splits, recon, part);
 }
 
-template <int K, bool H>
+template <int K, bool H, bool COMP>
 void fwd_tiled_kind(const TileMatrixDev& T, int g, int len_kind, float inv_scale,
-                    const float* recon, float* sim, cudaStream_t st) {
+                    const float* recon, float* part, cudaStream_t st) {
   switch (len_kind) {
-    case LK_F32: fwd_tiled_launch<K, LK_F32, H>(T, g, inv_scale, recon, sim, st); break;
-    case LK_BF16: fwd_tiled_launch<K, LK_BF16, H>(T, g, inv_scale, recon, sim, st); break;
-    case LK_F16: fwd_tiled_launch<K, LK_F16, H>(T, g, inv_scale, recon, sim, st); break;
-    default: fwd_tiled_launch<K, LK_U16, H>(T, g, inv_scale, recon, sim, st); break;
+    case LK_F32: fwd_tiled_launch<K, LK_F32, H, COMP>(T, g, inv_scale, recon, part, st); break;
+    case LK_BF16: fwd_tiled_launch<K, LK_BF16, H, COMP>(T, g, inv_scale, recon, part, st); break;
+    case LK_F16: fwd_tiled_launch<K, LK_F16, H, COMP>(T, g, inv_scale, recon, part, st); break;
+    default: fwd_tiled_launch<K, LK_U16, H, COMP>(T, g, inv_scale, recon, part, st); break;
   }
+}
+
+template <int K, bool COMP>
+void fwd_tiled_half(const IterArgs& A, const TileMatrixDev& T, const float* recon,
+                    float* part, cudaStream_t st) {
+  // an f32 tile of 16 slices would not fit shared memory (plan creation
+  // requires half_gathers with 16 slices per pass and forward_tiles)
+  if (K == 16 || A.half_tile)
+    fwd_tiled_kind<K, true, COMP>(T, A.G.C, A.M.len_kind, A.M.inv_scale, recon, part, st);
+  else if constexpr (K != 16)
+    fwd_tiled_kind<K, false, COMP>(T, A.G.C, A.M.len_kind, A.M.inv_scale, recon, part, st);
 }
 
 template <int K>
-void fwd_tiled_half(const IterArgs& A, const TileMatrixDev& T, const float* recon,
-                    float* sim, cudaStream_t st) {
-  if constexpr (K == 16) {
-    // an f32 tile of 16 slices would not fit shared memory (plan creation
-    // requires half_gathers with 16 slices per pass and forward_tiles)
-    fwd_tiled_kind<K, true>(T, A.G.C, A.M.len_kind, A.M.inv_scale, recon, sim, st);
-  } else if (A.half_tile) {
-    fwd_tiled_kind<K, true>(T, A.G.C, A.M.len_kind, A.M.inv_scale, recon, sim, st);
-  } else {
-    fwd_tiled_kind<K, false>(T, A.G.C, A.M.len_kind, A.M.inv_scale, recon, sim, st);
-  }
+void fwd_tiled_comp(const IterArgs& A, const TileMatrixDev& T, const float* recon,
+                    float* part, cudaStream_t st) {
+  if (A.comp) fwd_tiled_half<K, true>(A, T, recon, part, st);
+  else fwd_tiled_half<K, false>(A, T, recon, part, st);
 }
 
 inline int blocks_for(int64_t n, int b) { return (int)((n + b - 1) / b); }
@@ -564,12 +608,13 @@ int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
 void launch_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
                        int64_t nruns, const int* tile_first_run,
                        const int* group_first, const uint16_t* run_lp,
-                       const uint16_t* run_len, int* gray, uint16_t* glp,
+                       const uint16_t* run_len, const int64_t* ray_run_off,
+                       const int* pbase, int* gpart, uint16_t* glp,
                        uint16_t* glen, int* gsteps, int* run_slot,
                        cudaStream_t st) {
   k_runs_group<<<blocks_for(nruns, 256), 256, 0, st>>>(
-      rk, skey, sval, nruns, tile_first_run, group_first, run_lp, run_len, gray, glp,
-      glen, gsteps, run_slot);
+      rk, skey, sval, nruns, tile_first_run, group_first, run_lp, run_len, ray_run_off,
+      pbase, gpart, glp, glen, gsteps, run_slot);
 }
 
 template <bool L16>
@@ -607,35 +652,41 @@ void launch_runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x,
 }
 
 void launch_forward_tiled(const IterArgs& A, const TileMatrixDev& T,
-                          const float* recon_batch, float* sim, cudaStream_t st) {
+                          const float* recon_batch, float* part, cudaStream_t st) {
   switch (A.K) {
-    case 1: fwd_tiled_half<1>(A, T, recon_batch, sim, st); break;
-    case 2: fwd_tiled_half<2>(A, T, recon_batch, sim, st); break;
-    case 4: fwd_tiled_half<4>(A, T, recon_batch, sim, st); break;
-    case 8: fwd_tiled_half<8>(A, T, recon_batch, sim, st); break;
-    default: fwd_tiled_half<16>(A, T, recon_batch, sim, st); break;
+    case 1: fwd_tiled_comp<1>(A, T, recon_batch, part, st); break;
+    case 2: fwd_tiled_comp<2>(A, T, recon_batch, part, st); break;
+    case 4: fwd_tiled_comp<4>(A, T, recon_batch, part, st); break;
+    case 8: fwd_tiled_comp<8>(A, T, recon_batch, part, st); break;
+    default: fwd_tiled_comp<16>(A, T, recon_batch, part, st); break;
   }
 }
 
 template <int K>
-void fwd_finish_k(const IterArgs& A, float* sim, const float* sino, float* out,
-                  int out_mode, cudaStream_t st) {
+void fwd_finish_k(const IterArgs& A, const TileMatrixDev& T, const float* part,
+                  const float* sino, float* out, int out_mode, cudaStream_t st) {
   const int64_t R = (int64_t)A.G.P * A.G.C;
   const int b = blocks_for(R, 256);
-  if (A.half_factors && out_mode == FWD_RATIO)
-    k_fwd_finish<K, true><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode);
-  else
-    k_fwd_finish<K, false><<<b, 256, 0, st>>>(R, A.M.ra2, sim, sino, out, out_mode);
+#define TG_FINISH(FH, CP)                                                     \
+  k_fwd_finish<K, FH, CP><<<b, 256, 0, st>>>(R, T.rnrun, T.pbase, A.M.ra2, part, sino, \
+                                             out, out_mode)
+  const bool fh = A.half_factors && out_mode == FWD_RATIO;
+  if (A.comp) {
+    if (fh) TG_FINISH(true, true); else TG_FINISH(false, true);
+  } else {
+    if (fh) TG_FINISH(true, false); else TG_FINISH(false, false);
+  }
+#undef TG_FINISH
 }
 
-void launch_fwd_finish(const IterArgs& A, float* sim, const float* sino,
-                       float* out, int out_mode, cudaStream_t st) {
+void launch_fwd_finish(const IterArgs& A, const TileMatrixDev& T, const float* part,
+                       const float* sino, float* out, int out_mode, cudaStream_t st) {
   switch (A.K) {
-    case 1: fwd_finish_k<1>(A, sim, sino, out, out_mode, st); break;
-    case 2: fwd_finish_k<2>(A, sim, sino, out, out_mode, st); break;
-    case 4: fwd_finish_k<4>(A, sim, sino, out, out_mode, st); break;
-    case 8: fwd_finish_k<8>(A, sim, sino, out, out_mode, st); break;
-    default: fwd_finish_k<16>(A, sim, sino, out, out_mode, st); break;
+    case 1: fwd_finish_k<1>(A, T, part, sino, out, out_mode, st); break;
+    case 2: fwd_finish_k<2>(A, T, part, sino, out, out_mode, st); break;
+    case 4: fwd_finish_k<4>(A, T, part, sino, out, out_mode, st); break;
+    case 8: fwd_finish_k<8>(A, T, part, sino, out, out_mode, st); break;
+    default: fwd_finish_k<16>(A, T, part, sino, out, out_mode, st); break;
   }
 }
 

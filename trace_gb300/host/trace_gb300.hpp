@@ -47,6 +47,7 @@ struct Options {
   int backward_staged = 0;  // fast mode: shared-memory detector windows
   int half_gathers = 0;     // fast mode + forward_tiles: 16-bit gather operands
   int forward_on_the_fly = 0;  // trace rays during the forward projection
+  int compensated = 0;      // fast mode + forward_tiles: Kahan ray/pixel sums
 };
 
 // Geometry + reconstruction (TraceMetadata). theta is copied, not owned.
@@ -82,6 +83,7 @@ class GpuTraceMetadata {
     d.backward_staged = opt.backward_staged;
     d.half_gathers = opt.half_gathers;
     d.forward_on_the_fly = opt.forward_on_the_fly;
+    d.compensated = opt.compensated;
     tg_plan* p = nullptr;
     check(tg_plan_create(&d, theta, nullptr, nullptr, &p), nullptr);
     plan_.reset(p);

@@ -11,6 +11,7 @@
 //               [-m delta1] [-w regw] [--degrees] [--fused]
 //               [--len u16|f16|bf16|f32] [--slices-per-pass K] [--fast]
 //               [--delta-index] [--apmlr-fixed-offset] [--tiles] [--half]
+//               [--compensated]
 //               [--on-the-fly]
 //
 // sino is [P][S][C] (the /exchange/data order), theta holds P angles in
@@ -37,7 +38,7 @@ struct Config {
   float center = 0.f, beta = 10.f, beta1 = 1.f, delta = 1.f, delta1 = 1.f,
         regw = 1.f;
   bool degrees = false, fused = false, fast = false, delta_index = false,
-       fixed = false, tiles = false, half = false, otf = false;
+       fixed = false, tiles = false, half = false, otf = false, comp = false;
   int len = TG_LEN_F32;
 };
 
@@ -81,6 +82,7 @@ Config parse(int argc, char** argv) {
     else if (a == "--tiles") c.tiles = true;
     else if (a == "--half") c.half = true;
     else if (a == "--on-the-fly") c.otf = true;
+    else if (a == "--compensated") c.comp = true;
     else if (a == "--slices-per-pass") c.spp = std::stoi(next());
     else if (a == "--len") {
       const std::string v = next();
@@ -109,6 +111,7 @@ void run(const Config& cfg, int alg, std::vector<float>& theta,
   opt.forward_tiles = cfg.tiles;
   opt.half_gathers = cfg.half;
   opt.forward_on_the_fly = cfg.otf;
+  opt.compensated = cfg.comp;
   // MLEM/PML/APMLR drivers apply Absolute and start from 1 (mlem_main.cc:115,
   // 134); APMLR keeps one neighbour slice on each side (apmlr_main.cc:170).
   GpuTraceMetadata trace_metadata(theta.data(), 0, 0, 0, cfg.S, cfg.P, cfg.S,
