@@ -437,6 +437,8 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
         K, args.tiles, args.staged = (best["slices_per_pass"], best["forward_tiles"],
                                       best["backward_staged"])
         args.otf = best.get("forward_on_the_fly", False)
+        args.fts = best.get("forward_tile_side", 0)
+        args.btw = best.get("backward_tile_width", 0)
         args.slices_per_pass = K
         tuned = {"chosen": best, "sample_slices": n,
                  "ms_per_slice_iter": [[c, round(ms, 4)] for c, ms, _, _ in res]}
@@ -449,7 +451,8 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
     plan = tg.Plan(P, S, C, theta, len_storage=args.len_storage, slices_per_pass=K,
                    mode="fast", delta_index=True, forward_tiles=args.tiles,
                    backward_staged=args.staged, half_gathers=args.half,
-                   forward_on_the_fly=args.otf)
+                   forward_on_the_fly=args.otf, compensated=args.compensated,
+                   forward_tile_side=args.fts, backward_tile_width=args.btw)
     plan.set_stream(stream)
     info = plan.info()
     sino = make_data(W, dev, plan)
@@ -561,10 +564,13 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
                    "len_storage": args.len_storage, "index": "4-bit delta",
                    "gather_operands": "f16 (tile, factor-1)" if args.half else "f32",
                    "intersections": "traced on the fly" if args.otf else "cached",
-                   "forward": "tile-staged (64x64 shared-memory tiles)" if args.tiles
-                              else "ray-ordered",
+                   "forward": (f"tile-staged ({args.fts or 64}x{args.fts or 64} "
+                               "shared-memory tiles)") if args.tiles else "ray-ordered",
+                   "backward_tile": {4: "4x8", 16: "16x2"}.get(args.btw, "8x4") + " pixels",
                    "step": f"one {alg.upper()} iteration over all {S} slices",
                    "graphs": bool(args.graphs),
+                   "summation": "compensated (Kahan over 8-segment / 4-angle blocks)"
+                                if args.compensated else "FMA chains",
                    "l2": "inputs larger than L2 (system matrix "
                          f"{(info['forward_bytes'] + info['backward_bytes']) / 1e9:.1f} GB "
                          "streamed per step)",
@@ -614,10 +620,14 @@ def fp64_check(args, W, theta, sino, prm, tg, torch, dev):
         # subset fills one batch)
         "mixed": dict(len_storage=args.len_storage, mode="fast", delta_index=True,
                       forward_tiles=args.tiles, backward_staged=args.staged,
-                      half_gathers=args.half, slices_per_pass=args.slices_per_pass),
+                      half_gathers=args.half, slices_per_pass=args.slices_per_pass,
+                      compensated=args.compensated, forward_tile_side=args.fts,
+                      backward_tile_width=args.btw),
         "fp32_same_schedule": dict(len_storage="f32", mode="fast", delta_index=True,
                                    forward_tiles=args.tiles, backward_staged=args.staged,
-                                   slices_per_pass=args.slices_per_pass),
+                                   slices_per_pass=args.slices_per_pass,
+                                   backward_tile_width=args.btw,
+                                   compensated=args.compensated),
         "plain_fp32": dict(len_storage="f32", mode="exact"),
     }
     runs = {}
@@ -653,7 +663,7 @@ def fp32_same_schedule(args, W, theta, sino, prm, tg, torch, stream):
     p = tg.Plan(W["P"], n, W["C"], theta, len_storage="f32",
                 slices_per_pass=args.slices_per_pass, mode="fast", delta_index=True,
                 forward_tiles=args.tiles, backward_staged=args.staged,
-                forward_on_the_fly=args.otf)
+                forward_on_the_fly=args.otf, backward_tile_width=args.btw)
     p.set_stream(stream)
     p.set_graphs(True)
     info = p.info()
@@ -714,7 +724,9 @@ def end_to_end(args, W, theta, sino, prm, tg, torch, stream):
         p = tg.Plan(W["P"], W["S"], W["C"], theta, len_storage=args.len_storage,
                     slices_per_pass=args.slices_per_pass, mode="fast",
                     delta_index=True, forward_tiles=args.tiles,
-                    backward_staged=args.staged, half_gathers=args.half)
+                    backward_staged=args.staged, half_gathers=args.half,
+                    forward_on_the_fly=args.otf, compensated=args.compensated,
+                    forward_tile_side=args.fts, backward_tile_width=args.btw)
         p.set_stream(stream)
         p.set_graphs(args.graphs)
         upload(p, W, host)
@@ -754,12 +766,40 @@ def batch_problems_with_theta(W):
     return probs
 
 
-def batch_plan_kw(pr, args):
+def batch_plan_kw(pr, args, tuned=None):
+    """Plan options of one batch problem: 16-bit lengths, tile-staged forward,
+    slices per pass the largest power of two <= min(8, slices), and the tile
+    side and backprojection tile shape autotuned for its detector width."""
     K = 1
     while K * 2 <= min(8, pr["S"]):
         K *= 2
-    return dict(len_storage="u16", slices_per_pass=K, mode="fast", delta_index=True,
-                forward_tiles=True, half_gathers=args.half)
+    kw = dict(len_storage="u16", slices_per_pass=K, mode="fast", delta_index=True,
+              forward_tiles=True, half_gathers=args.half)
+    if tuned and pr["C"] in tuned:
+        kw.update(tuned[pr["C"]])
+    return kw
+
+
+def batch_autotune(args, probs, hosts, stream):
+    """Per detector width: the forward tile side and backprojection tile shape
+    that the autotuner measures fastest on that width's problem with the most
+    angles (its slices, its algorithm)."""
+    from trace_gb300.autotune import autotune
+    tuned, log = {}, {}
+    for C in sorted(set(pr["C"] for pr in probs)):
+        i = max((j for j, pr in enumerate(probs) if pr["C"] == C),
+                key=lambda j: probs[j]["P"])
+        pr = probs[i]
+        kw = batch_plan_kw(pr, args)
+        best, res = autotune(pr["theta"], hosts[i], pr["alg"], len_storage="u16",
+                             space={"slices_per_pass": (kw["slices_per_pass"],),
+                                    "forward_tiles": (True,)},
+                             fixed={"half_gathers": args.half}, stream=stream)
+        tuned[C] = {k: best[k] for k in ("forward_tile_side", "backward_tile_width")
+                    if k in best}
+        log[str(C)] = {"problem": i, "chosen": tuned[C],
+                       "ms_per_slice_iter": [[c, round(ms, 4)] for c, ms, _, _ in res]}
+    return tuned, log
 
 
 def batch_estimate_bytes(pr):
@@ -801,6 +841,9 @@ def run_batch(args, W):
         outs_host = [torch.empty((pr["S"], pr["C"], pr["C"]), dtype=torch.float32).pin_memory()
                      for pr in probs]
         torch.cuda.synchronize()
+        tuned, tune_log = (batch_autotune(args, probs, hosts, stream) if args.autotune
+                           else (None, None))
+        args.batch_tuned = tuned
         budget = args.batch_budget_gb * 1e9
         waves, cur, used = [], [], 0.0
         for i, pr in enumerate(probs):
@@ -814,6 +857,7 @@ def run_batch(args, W):
         iters = W["iters"]
         e2e_s = iter_ms = setup_ms = alg_bytes = 0.0
         timed_slice_iters = launches = h2d = d2h = 0
+        multi = True
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         with ClockSampler(local) as clk:
@@ -823,7 +867,8 @@ def run_batch(args, W):
                 plans = []
                 for i in wave:
                     pr = probs[i]
-                    p = tg.Plan(pr["P"], pr["S"], pr["C"], pr["theta"], **batch_plan_kw(pr, args))
+                    p = tg.Plan(pr["P"], pr["S"], pr["C"], pr["theta"],
+                                **batch_plan_kw(pr, args, tuned))
                     p.set_stream(stream)
                     p.set_sinogram(hosts[i], apply_abs=pr["alg"] != "sirt")
                     p.reset_recon(pr["alg"])
@@ -832,10 +877,12 @@ def run_batch(args, W):
                     h2d += hosts[i].numel() * 4
                 algs = [probs[i]["alg"] for i in wave]
                 batch = tg.Batch(plans)
-                batch.iterate(algs, 1)  # first iteration: captures the graph
+                batch.iterate(algs, 1)  # first iteration: captures its graph
                 ev0.record()
                 batch.iterate(algs, iters - 1)
                 ev1.record()
+                binfo = batch.info()
+                multi = multi and binfo["multi"]
                 outs = [p.get_recon(probs[i]["alg"], out=outs_host[i])
                         for p, i in zip(plans, wave)]
                 torch.cuda.synchronize()
@@ -845,12 +892,12 @@ def run_batch(args, W):
                     pr = probs[i]
                     info = p.info()
                     timed_slice_iters += pr["S"] * (iters - 1)
-                    launches += (iters - 1) * info["batches"] * 3
-                    K = batch_plan_kw(pr, args)["slices_per_pass"]
+                    K = batch_plan_kw(pr, args, tuned)["slices_per_pass"]
                     fb, bb = kernel_bytes(info, dict(C=pr["C"], P=pr["P"], alg=pr["alg"]),
                                           K, "u16")
                     alg_bytes += (iters - 1) * info["batches"] * (fb + bb)
                 d2h += sum(o.numel() * 4 for o in outs)
+                launches += (iters - 1) * binfo["launches"]
                 batch.close()
                 for p in plans:
                     p.close()
@@ -859,6 +906,10 @@ def run_batch(args, W):
     value = timed_slice_iters * ws / (ms_max / 1e3)
     total_slice_iters = sum(pr["S"] for pr in probs) * W["iters"]
     achieved = alg_bytes / (iter_ms / 1e3) / 1e9
+    rel = None
+    if args.fp64_check and rank == 0:
+        with torch.cuda.stream(ts):
+            rel = batch_fp64_check(args, W, probs, hosts, outs_host, tg, torch, ts.cuda_stream)
     cpu = None
     if args.cpu_baseline and rank == 0 and ws == 1:
         cpu = batch_cpu_baseline(W, probs)
@@ -874,8 +925,13 @@ def run_batch(args, W):
         "data": "synthetic: seeded random ellipses projected by the plan's projector",
         "config": {"workload": W["name"], "problems": len(probs),
                    "waves": len(waves), "wave_budget_gb": args.batch_budget_gb,
-                   "step": "one iteration of every problem of a wave, one CUDA-graph "
-                           "launch (plans forked over up to 16 streams inside the graph)",
+                   "step": ("one iteration of every problem of a wave: one CUDA graph of "
+                            "multi-plan launches (per slice-batch round, one launch per "
+                            "kernel variant whose blocks walk all problems' tiles and rays)")
+                           if multi else
+                           ("one iteration of every problem of a wave, one CUDA-graph launch "
+                            "(plans forked over up to 16 streams inside the graph)"),
+                   "multi_plan_launches": multi,
                    "slices_per_pass": "largest power of two <= min(8, slices)",
                    "l2": "inputs larger than L2 (system matrices streamed per step)",
                    "parallelism": f"replicas x{ws}"},
@@ -884,7 +940,7 @@ def run_batch(args, W):
                      "peak_kind": f"{peak_kind} (burst copy)", "traffic": None,
                      "kernel": "all kernels of the batch (whole-step effective bandwidth)"},
         "clocks": clk.summary(), "gpu_launches": launches,
-        "setup_ms": setup_ms,
+        "setup_ms": setup_ms, "rel_l2_vs_fp64": rel, "autotune": tune_log,
         "e2e": {"value": total_slice_iters / e2e_s, "unit": "slice-iter/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "step": "every wave: plan creation (tracing), upload from pinned host, "
@@ -892,6 +948,45 @@ def run_batch(args, W):
         "cpu_baseline": cpu, "wall_s": time.time() - t_start,
     }
     print(json.dumps(line), flush=True)
+
+
+def batch_fp64_check(args, W, probs, hosts, outs_host, tg, torch, stream, sample=8):
+    """Relative L2 against the GPU FP64 mode for a seeded sample of the
+    batch's problems: per iteration, from a plan with the batch's
+    configuration iterated alone (the multi-plan launches give its results
+    bit for bit), and for the final reconstruction the batch delivered."""
+    import numpy as np
+    rng = np.random.default_rng(W["seed"] + 2)
+    idx = sorted(rng.choice(len(probs), sample, replace=False).tolist())
+    out = {"problems": [], "reference": "GPU FP64 mode", "iterations": W["iters"]}
+    worst = 0.0
+    for i in idx:
+        pr = probs[i]
+        runs = {}
+        for key, kw in (("fp64", dict(len_storage="f32", mode="fp64")),
+                        ("mixed", batch_plan_kw(pr, args, getattr(args, "batch_tuned", None)))):
+            p = tg.Plan(pr["P"], pr["S"], pr["C"], pr["theta"], **kw)
+            p.set_stream(stream)
+            p.set_sinogram(hosts[i], apply_abs=pr["alg"] != "sirt")
+            p.reset_recon(pr["alg"])
+            snaps = []
+            for _ in range(W["iters"]):
+                p.iterate(pr["alg"], 1)
+                snaps.append(p.get_recon(pr["alg"]))
+            runs[key] = snaps
+            p.close()
+        errs = [float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b))
+                for a, b in zip(runs["mixed"], runs["fp64"])]
+        final_batch = outs_host[i].numpy()
+        eb = float(np.linalg.norm(final_batch.astype(np.float64) - runs["fp64"][-1])
+                   / np.linalg.norm(runs["fp64"][-1]))
+        worst = max(worst, max(errs), eb)
+        out["problems"].append({"index": i, "alg": pr["alg"], "C": pr["C"], "P": pr["P"],
+                                "S": pr["S"], "max": max(errs), "final": errs[-1],
+                                "batch_final": eb})
+        torch.cuda.empty_cache()
+    out["max"] = worst
+    return out
 
 
 def batch_cpu_baseline(W, probs, sample=4):
@@ -939,9 +1034,15 @@ def main():
     ap.add_argument("--on-the-fly", dest="otf", action="store_true",
                     help="no stored ray-ordered forward matrix: rays traced during "
                          "forward projections")
-    ap.add_argument("--autotune", action="store_true",
-                    help="time the plan configurations on a 16-slice sample first "
-                         "and run the fastest")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="skip timing the plan configurations on a 16-slice sample "
+                         "(run the defaults or the flags given)")
+    ap.add_argument("--forward-tile-side", dest="fts", type=int, default=0,
+                    help="forward tile side (32, 64, 96; 0 = the plan default)")
+    ap.add_argument("--backward-tile-width", dest="btw", type=int, default=0,
+                    help="backprojection tile width (4, 8, 16; 0 = the plan default)")
+    ap.add_argument("--compensated", action="store_true",
+                    help="compensated (Kahan) ray and pixel sums in the measured path")
     ap.add_argument("--no-graphs", dest="graphs", action="store_false",
                     help="eager launches instead of one CUDA graph per iteration")
     ap.add_argument("--no-plain", dest="plain", action="store_false")

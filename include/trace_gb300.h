@@ -126,12 +126,21 @@ typedef struct {
                              projections use the tile-ordered matrix and the
                              option only saves memory (the tile build traces
                              instead of reading the ray-ordered matrix) */
-  int compensated;        /* fast mode with forward_tiles and the L1
-                             backprojection: compensated (Kahan) summation -
+  int compensated;        /* fast mode with forward_tiles, the L1
+                             backprojection and at most 8 slices per pass:
+                             compensated (Kahan) summation -
                              each ray's sum in blocks of 8 segments within a
                              tile run and across its runs, each pixel's
                              backprojection sum in blocks of 4 angles; the
                              blocks themselves are FMA chains */
+  int backward_tile_width; /* pixels per warp row of the backward matrix and
+                              backprojection: 8 (8x4 tiles; 0 selects it),
+                              16 (16x2) or 4 (4x8); backward_staged needs 8 */
+  int forward_tile_side;   /* forward_tiles: side of the shared-memory
+                              reconstruction tiles, 32, 64 (0 selects it) or
+                              96; the tile of slices_per_pass slices must fit
+                              shared memory (96 needs half_gathers and at
+                              most 8 slices per pass) */
 } tg_plan_desc;
 
 typedef struct {
@@ -244,13 +253,19 @@ int tg_iterate(tg_plan* plan, int alg, const tg_params* params, int n_iter);
  * per-kernel timers are on. */
 int tg_plan_set_graphs(tg_plan* plan, int enable);
 
-/* A batch of independent plans (any geometries) iterated together: each
- * iteration of every plan is captured into one CUDA graph whose branches
- * run on up to 16 streams, so one graph launch advances all of them - the
- * counterpart of running many drivers (or MPI ranks over disjoint slice
- * blocks, trace_h5io.cc:7-22) side by side. Plans must be ready to iterate
- * (layout, sinogram) and stay owned by the caller. tg_batch_iterate returns
- * after the work has finished. */
+/* A batch of independent plans (any geometries and slice counts) iterated
+ * together - the counterpart of running many drivers (or MPI ranks over
+ * disjoint slice blocks, trace_h5io.cc:7-22) side by side. Plans must be
+ * ready to iterate (layout, sinogram) and stay owned by the caller.
+ * When every plan is fast mode with forward_tiles, the L1 backprojection
+ * and TG_LEN_U16 lengths, one iteration of all plans is, per round of slice
+ * batches, one launch of each kernel variant (tile-staged forward, finish,
+ * fused backprojection + update; variants by slices per pass, gather
+ * precision, penalty, summation) whose blocks walk a work list spanning
+ * every plan's tiles and rays; otherwise each plan's own launches are
+ * branches of one graph over up to 16 streams. Either way each iteration
+ * replays a captured CUDA graph, and results equal tg_iterate's bit for
+ * bit. tg_batch_iterate returns after the work has finished. */
 typedef struct tg_batch tg_batch;
 int tg_batch_create(tg_plan* const* plans, int n, tg_batch** out);
 int tg_batch_iterate(tg_batch* batch, const int* algs, const tg_params* params,
@@ -258,6 +273,10 @@ int tg_batch_iterate(tg_batch* batch, const int* algs, const tg_params* params,
 int tg_batch_synchronize(tg_batch* batch);
 int tg_batch_destroy(tg_batch* batch);
 const char* tg_batch_last_error(const tg_batch* batch);
+/* *multi: 1 when iterations use the multi-plan launches above;
+ * *launches: kernel launches per iteration of the last tg_batch_iterate
+ * (0 before the first). Either pointer may be NULL. */
+int tg_batch_get_info(const tg_batch* batch, int* multi, int* launches);
 
 /* Forward projection of the current reconstruction: sim [P][S][C]. */
 int tg_forward_project(tg_plan* plan, int alg, const tg_params* params,

@@ -80,3 +80,60 @@ def test_plans_created_from_host_threads():
         threaded = list(ex.map(run, cases))
     for a, b in zip(serial, threaded):
         assert np.array_equal(bits(a), bits(b))
+
+
+MULTI_SPECS = [  # (C, P, S, alg, slices per pass, half gathers, compensated)
+    (64, 40, 3, "sirt", 2, True, False), (96, 70, 9, "mlem", 8, True, False),
+    (48, 33, 5, "pml", 4, True, False), (80, 25, 1, "mlem", 1, False, False),
+    (130, 90, 16, "sirt", 16, True, False), (72, 61, 7, "apmlr", 4, True, False),
+    (100, 45, 6, "mlem", 8, True, True), (64, 50, 4, "pml", 4, False, True),
+]
+
+
+def test_batch_multi_plan_launches_match_individual_plans():
+    """Fast tile-staged plans with 16-bit lengths advance together through the
+    multi-plan launches (one per kernel variant and slice-batch round, blocks
+    walking every plan's work): bit-identical to each plan iterated alone,
+    from a fresh reconstruction (FP32-factor first iteration) on, across
+    calls (buffer parity), with far fewer launches than per-plan kernels."""
+    def mk(i, spec):
+        C, P, S, alg, K, half, comp = spec
+        return _plan(C, P, S, 30 + i, alg, slices_per_pass=K, mode="fast",
+                     len_storage="u16", delta_index=True, forward_tiles=True,
+                     half_gathers=half, compensated=comp)
+    algs = [s[3] for s in MULTI_SPECS]
+    prms = [tg.default_params(a, beta=0.4) for a in algs]
+    singles = []
+    for i, spec in enumerate(MULTI_SPECS):
+        plan = mk(i, spec)
+        plan.iterate(algs[i], 4, prms[i])
+        singles.append(plan.get_recon(algs[i]))
+        plan.close()
+    plans = [mk(i, spec) for i, spec in enumerate(MULTI_SPECS)]
+    batch = tg.Batch(plans)
+    batch.iterate(algs, 1, prms)
+    batch.iterate(algs, 2, prms)
+    batch.iterate(algs, 1, prms)
+    info = batch.info()
+    assert info["multi"]
+    per_plan = sum(p.info()["batches"] * 3 for p in plans)
+    assert 0 < info["launches"] < per_plan
+    for plan, alg, want in zip(plans, algs, singles):
+        assert np.array_equal(bits(plan.get_recon(alg)), bits(want))
+    batch.close()
+    for p in plans:
+        p.close()
+
+
+def test_batch_with_an_ineligible_plan_uses_per_plan_graph():
+    plans = [_plan(64, 40, 3, 1, "sirt", slices_per_pass=2, mode="fast", len_storage="u16",
+                   delta_index=True, forward_tiles=True),
+             _plan(48, 30, 2, 2, "sirt", slices_per_pass=1)]  # exact mode
+    batch = tg.Batch(plans)
+    batch.iterate("sirt", 2)
+    assert not batch.info()["multi"]
+    assert batch.info()["launches"] == sum(p.info()["batches"] * (3 if i == 0 else 2)
+                                           for i, p in enumerate(plans))
+    batch.close()
+    for p in plans:
+        p.close()

@@ -198,3 +198,119 @@ def test_operator_path_uses_tiles(alg):
     assert rel_l2(reps[1], reps[0]) < 1e-6
     assert rel_l2(recons[1], recons[0]) < 1e-6
     assert rel_l2(sims[1], sims[0]) < 1e-6
+
+
+@pytest.mark.parametrize("alg", ["sirt", "mlem", "pml"])
+@pytest.mark.parametrize("storage,half", [("f32", False), ("u16", True)])
+def test_compensated_sums_against_fp64(alg, storage, half):
+    """compensated=1 (Kahan ray sums over 8-segment blocks and across tile
+    runs, Kahan pixel sums over 4-angle blocks): within 1e-4 of the FP64
+    oracle like the plain sums and bit-reproducible; with f32 storage, where
+    summation is the error left, no further from FP64 than the plain sums
+    (beyond 1e-7 of slack); with 16-bit storage, whose quantisation
+    dominates, within 5 % of their error."""
+    C, P, S, it = 128, 120, 8, 6
+    th = theta_uniform(P)
+    tabs = O.angle_table(th)
+    from trace_gb300.phantom import ellipse_phantoms
+    sino = O.forward(ellipse_phantoms(C, S, seed=21, texture_sigma=0.02), tabs)
+    kw = dict(beta=0.05) if alg == "pml" else {}
+    ref = O.run(alg, sino, tables=tabs, n_iter=it, precision=O.F64, **kw)["recon"]
+    prm = tg.default_params(alg, beta=0.05)
+    outs = {}
+    for comp in (False, True, True):
+        plan = tg.Plan(P, S, C, th, slices_per_pass=8, mode="fast", len_storage=storage,
+                       delta_index=True, forward_tiles=True, half_gathers=half,
+                       compensated=comp)
+        plan.set_sinogram(sino, apply_abs=alg != "sirt")
+        plan.reset_recon(alg)
+        plan.iterate(alg, it, prm)
+        out = plan.get_recon(alg)
+        plan.close()
+        if comp in outs:
+            assert np.array_equal(bits(out), bits(outs[comp]))
+        outs[comp] = out
+    e_plain, e_comp = rel_l2(outs[False], ref), rel_l2(outs[True], ref)
+    assert e_comp < 1e-4, (e_plain, e_comp)
+    if storage == "f32":
+        assert e_comp <= e_plain + 1e-7, (e_plain, e_comp)
+    else:
+        assert abs(e_comp - e_plain) <= 0.05 * e_plain, (e_plain, e_comp)
+
+
+@pytest.mark.parametrize("kw", [dict(mode="exact", forward_tiles=False),
+                                dict(mode="fast", forward_tiles=False),
+                                dict(mode="fast", forward_tiles=True, backward_staged=True)])
+def test_compensated_needs_tiles_and_l1_backprojection(kw):
+    with pytest.raises(tg.TraceError) as e:
+        tg.Plan(8, 1, 16, theta_uniform(8), compensated=True, **kw)
+    assert e.value.status == 1
+
+
+@pytest.mark.parametrize("kw", [dict(mode="exact"),
+                                dict(mode="fast", len_storage="u16", delta_index=True,
+                                     slices_per_pass=8, forward_tiles=True,
+                                     half_gathers=True)])
+@pytest.mark.parametrize("alg", ["sirt", "mlem", "pml", "apmlr"])
+def test_backward_tile_shapes_are_bit_identical(kw, alg):
+    """The backprojection's pixel tile (8x4 default, 16x2, 4x8) only decides
+    which warp owns a pixel; every pixel sums its angles in the same order,
+    so the results are bit-identical (an odd grid, uneven tiles)."""
+    C, P, S = 99, 70, 5
+    th = theta_uniform(P)
+    rng = np.random.default_rng(41)
+    sino = rng.uniform(0.5, 2.0, (P, S, C)).astype(np.float32)
+    prm = tg.default_params(alg, beta=0.2)
+    outs = []
+    for tw in (0, 16, 4):
+        plan = tg.Plan(P, S, C, th, backward_tile_width=tw, **kw)
+        plan.set_sinogram(sino, apply_abs=alg != "sirt")
+        plan.reset_recon(alg)
+        plan.iterate(alg, 3, prm)
+        outs.append(plan.get_recon(alg))
+        plan.close()
+    assert np.array_equal(bits(outs[1]), bits(outs[0]))
+    assert np.array_equal(bits(outs[2]), bits(outs[0]))
+
+
+@pytest.mark.parametrize("ts", [32, 96])
+@pytest.mark.parametrize("alg", ["sirt", "mlem", "pml"])
+def test_forward_tile_sides(ts, alg):
+    """Forward tiles of 32 or 96 pixels regroup each ray's sum by tile runs:
+    within 1e-6 of the 64-pixel tiles with FP32 operands, and the benchmark
+    configuration stays within 1e-4 of the FP64 oracle."""
+    C, P, S, it = 200, 150, 8, 5
+    th = theta_uniform(P)
+    tabs = O.angle_table(th)
+    from trace_gb300.phantom import ellipse_phantoms
+    sino = O.forward(ellipse_phantoms(C, S, seed=23, texture_sigma=0.02), tabs)
+    kw = dict(beta=0.05) if alg == "pml" else {}
+    ref = O.run(alg, sino, tables=tabs, n_iter=it, precision=O.F64, **kw)["recon"]
+    prm = tg.default_params(alg, beta=0.05)
+    res = {}
+    for side in (0, ts):
+        for half in (False, True):
+            if side == 96 and not half:
+                continue  # an f32 tile of 96 x 97 x 8 would not fit shared memory
+            plan = tg.Plan(P, S, C, th, slices_per_pass=8, mode="fast", len_storage="u16",
+                           delta_index=True, forward_tiles=True, half_gathers=half,
+                           forward_tile_side=side)
+            plan.set_sinogram(sino, apply_abs=alg != "sirt")
+            plan.reset_recon(alg)
+            plan.iterate(alg, it, prm)
+            res[(side, half)] = plan.get_recon(alg)
+            plan.close()
+    if (ts, False) in res:
+        assert rel_l2(res[(ts, False)], res[(0, False)]) < 1e-6
+    assert rel_l2(res[(ts, True)], ref) < 1e-4
+
+
+def test_forward_tile_that_does_not_fit_is_rejected():
+    with pytest.raises(tg.TraceError) as e:
+        tg.Plan(8, 8, 100, theta_uniform(8), slices_per_pass=8, mode="fast",
+                forward_tiles=True, forward_tile_side=96)  # f32 tile: 298 KB
+    assert e.value.status == 1
+    with pytest.raises(tg.TraceError) as e:
+        tg.Plan(8, 1, 100, theta_uniform(8), mode="fast", forward_tiles=True,
+                forward_tile_side=48)
+    assert e.value.status == 1

@@ -37,7 +37,7 @@ EXPORTED = [
     "tg_forward_project", "tg_trace_rays", "tg_plan_set_timing",
     "tg_plan_get_timing", "tg_plan_set_graphs", "tg_batch_create",
     "tg_batch_iterate", "tg_batch_synchronize", "tg_batch_destroy",
-    "tg_batch_last_error",
+    "tg_batch_last_error", "tg_batch_get_info",
 ]
 
 
@@ -55,7 +55,8 @@ class PlanDesc(C.Structure):
                 ("mode", C.c_int), ("delta_index", C.c_int),
                 ("apmlr_fixed_offset", C.c_int), ("forward_tiles", C.c_int),
                 ("backward_staged", C.c_int), ("half_gathers", C.c_int),
-                ("forward_on_the_fly", C.c_int), ("compensated", C.c_int)]
+                ("forward_on_the_fly", C.c_int), ("compensated", C.c_int),
+                ("backward_tile_width", C.c_int), ("forward_tile_side", C.c_int)]
 
 
 class Params(C.Structure):
@@ -133,7 +134,8 @@ class Plan:
                  delta_index=False, apmlr_fixed_offset=False, slice_id=0,
                  num_total_slices=None, sin_tab=None, cos_tab=None,
                  forward_tiles=False, backward_staged=False, half_gathers=False,
-                 forward_on_the_fly=False, compensated=False):
+                 forward_on_the_fly=False, compensated=False, backward_tile_width=0,
+                 forward_tile_side=0):
         self._lib = load_library()
         self.P, self.S, self.C = int(num_projs), int(num_slices), int(num_cols)
         d = PlanDesc(self.P, self.S, self.C, float(center), int(slice_id),
@@ -144,7 +146,8 @@ class Plan:
                      int(bool(delta_index)), int(bool(apmlr_fixed_offset)),
                      int(bool(forward_tiles)), int(bool(backward_staged)),
                      int(bool(half_gathers)), int(bool(forward_on_the_fly)),
-                     int(bool(compensated)))
+                     int(bool(compensated)), int(backward_tile_width),
+                     int(forward_tile_side))
         theta = np.ascontiguousarray(theta, np.float32)
         if theta.size != self.P:
             raise ValueError("theta must have num_projs entries")
@@ -349,6 +352,15 @@ class Batch:
         rc = self._lib.tg_batch_iterate(self._h, a, pr, int(n_iter))
         if rc:
             raise TraceError(rc, self._lib.tg_batch_last_error(self._h).decode())
+
+    def info(self) -> dict:
+        """multi: whether iterations use the multi-plan launches; launches:
+        kernel launches per iteration of the last iterate call."""
+        m, n = C.c_int(), C.c_int()
+        rc = self._lib.tg_batch_get_info(self._h, C.byref(m), C.byref(n))
+        if rc:
+            raise TraceError(rc, "tg_batch_get_info")
+        return {"multi": bool(m.value), "launches": n.value}
 
     def close(self):
         if getattr(self, "_h", None):

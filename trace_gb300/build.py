@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libtrace_gb300.so")
-SOURCES = ["tg_trace.cu", "tg_forward.cu", "tg_backward.cu", "tg_backward_k8.cu", "tg_backward_k16.cu", "tg_backward_staged.cu", "tg_iter.cu", "tg_fp64.cu", "tg_tiles.cu", "tg_plan.cu"]
+SOURCES = ["tg_trace.cu", "tg_forward.cu", "tg_backward.cu", "tg_backward_k4.cu", "tg_backward_k8.cu", "tg_backward_k16.cu", "tg_backward_staged.cu", "tg_iter.cu", "tg_fp64.cu", "tg_tiles.cu", "tg_plan.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1,7 +1,8 @@
 // Backprojection (pixel-driven) with the algorithms' UpdateRecon fused into
 // its epilogue.
 //
-// One thread per pixel, one warp per 8x4 pixel tile, eight tiles per block.
+// One thread per pixel, one warp per 32-pixel tile (8x4 by default; 16x2
+// or 4x8 as the plan chooses), eight tiles per block.
 // For every angle a thread reads the lengths of the (at most two) rays
 // through its pixel - one contiguous 32-lane row of the backward matrix per
 // warp - and gathers those rays' factors. The sum over angles in column
@@ -169,19 +170,22 @@ constexpr int min_blocks() {
 
 // COMP: compensated summation - each quad's (four angles') products are an
 // FMA chain added to the pixel's sum with Kahan's correction.
+// One block's work (8 pixel tiles, from tile block * kWarps);
+// s_coef: the block's kCoefChunk-entry shared buffer of window coefficients.
 template <int K, int LK, bool EXACT, bool PEN, bool FH, bool COMP>
-__global__ void __launch_bounds__(kBlock, (min_blocks<K, COMP>()))
-    k_backward(IterArgs A, int batch, const float* __restrict__ cur,
-               float* __restrict__ next, const float* __restrict__ upd,
-               float* __restrict__ rep_num, int epi) {
-  __shared__ float4 s_coef[kCoefChunk];
+__device__ __forceinline__ void backward_block(const IterArgs& A, int batch, int block,
+                                               const float* __restrict__ cur,
+                                               float* __restrict__ next,
+                                               const float* __restrict__ upd,
+                                               float* __restrict__ rep_num, int epi,
+                                               float4* s_coef) {
   const DevGeom& G = A.G;
   const int g = G.C;
   const int64_t g2 = (int64_t)g * g;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tile = blockIdx.x * kWarps + warp;
-  const int x = (tile % A.M.tiles_x) * 8 + (lane & 7);
-  const int y = (tile / A.M.tiles_x) * 4 + (lane >> 3);
+  const int tile = block * kWarps + warp;
+  int x, y;
+  tile_pixel(tile, lane, A.M.tiles_x, A.M.tw_shift, &x, &y);
   const bool valid = tile < A.M.ntiles && x < g && y < g;
   const int64_t p = (int64_t)y * g + x;
   const float xf = (float)x, yf = (float)y;
@@ -359,6 +363,50 @@ __global__ void __launch_bounds__(kBlock, (min_blocks<K, COMP>()))
   }
 }
 
+template <int K, int LK, bool EXACT, bool PEN, bool FH, bool COMP>
+__global__ void __launch_bounds__(kBlock, (min_blocks<K, COMP>()))
+    k_backward(IterArgs A, int batch, const float* __restrict__ cur,
+               float* __restrict__ next, const float* __restrict__ upd,
+               float* __restrict__ rep_num, int epi) {
+  __shared__ float4 s_coef[kCoefChunk];
+  backward_block<K, LK, EXACT, PEN, FH, COMP>(A, batch, blockIdx.x, cur, next, upd,
+                                              rep_num, epi, s_coef);
+}
+
+// Many plans' fused backprojection + update in one launch (fast mode):
+// block -> work item (a plan's slice batch).
+template <int K, int LK, bool PEN, bool FH, bool COMP>
+__global__ void __launch_bounds__(kBlock, (min_blocks<K, COMP>()))
+    k_backward_multi(const BackItem* __restrict__ items, int nitems) {
+  __shared__ float4 s_coef[kCoefChunk];
+  const BackItem& it = items[item_of(items, nitems, blockIdx.x)];
+  backward_block<K, LK, false, PEN, FH, COMP>(it.A, it.batch, (int)(blockIdx.x - it.first),
+                                              it.cur, it.next, it.upd, nullptr, EPI_UPDATE,
+                                              s_coef);
+}
+
+// Multi-plan launches for plans with 16-bit fixed-point lengths: their
+// backward matrix holds u16 codes, or IEEE halves with half gathers.
+template <int K>
+void back_multi(const BackItem* items, int n, int64_t blocks, int dlen_kind, int pen,
+                int fh, int comp, cudaStream_t st) {
+#define TG_BM(LKK, PN, FHH, CP) \
+  k_backward_multi<K, LKK, PN, FHH, CP><<<(unsigned)blocks, kBlock, 0, st>>>(items, n)
+  constexpr bool kComp = K <= 8;  // compensated sums: up to 8 slices per pass
+#define TG_BM_PC(LKK, FHH)                                                               \
+  do {                                                                                   \
+    if (pen) { if (kComp && comp) TG_BM(LKK, true, FHH, kComp); else TG_BM(LKK, true, FHH, false); } \
+    else { if (kComp && comp) TG_BM(LKK, false, FHH, kComp); else TG_BM(LKK, false, FHH, false); }   \
+  } while (0)
+  if (dlen_kind == LK_F16) {
+    if (fh) TG_BM_PC(LK_F16, true); else TG_BM_PC(LK_F16, false);
+  } else {
+    TG_BM_PC(LK_U16, false);
+  }
+#undef TG_BM_PC
+#undef TG_BM
+}
+
 template <int K, int LK>
 void back_launch(const IterArgs& A, int batch, const float* cur, float* next,
                  const float* upd, float* rep_num, int epi, cudaStream_t st) {
@@ -367,13 +415,15 @@ void back_launch(const IterArgs& A, int batch, const float* cur, float* next,
 #define TG_BACK(E, PN, FH, CP)                                                        \
   k_backward<K, LK, E, PN, FH, CP><<<blocks, kBlock, 0, st>>>(A, batch, cur, next, upd, \
                                                              rep_num, epi)
+  // compensated sums: up to 8 slices per pass (plan creation checks)
+  constexpr bool kComp = K <= 8;
   if (A.exact) {
     if (pen) TG_BACK(true, true, false, false); else TG_BACK(true, false, false, false);
-  } else if (A.comp) {
+  } else if (kComp && A.comp) {
     if (A.half_factors) {
-      if (pen) TG_BACK(false, true, true, true); else TG_BACK(false, false, true, true);
+      if (pen) TG_BACK(false, true, true, kComp); else TG_BACK(false, false, true, kComp);
     } else {
-      if (pen) TG_BACK(false, true, false, true); else TG_BACK(false, false, false, true);
+      if (pen) TG_BACK(false, true, false, kComp); else TG_BACK(false, false, false, kComp);
     }
   } else if (A.half_factors) {
     if (pen) TG_BACK(false, true, true, false); else TG_BACK(false, false, true, false);
@@ -403,6 +453,11 @@ void back_kind(const IterArgs& A, int batch, const float* cur, float* next,
                              float* recon_next, const float* upd, float* rep_num,      \
                              int epi, cudaStream_t st) {                               \
     back_kind<KK>(A, batch, recon_cur, recon_next, upd, rep_num, epi, st);             \
+  }                                                                                     \
+  void launch_backward_multi_k##KK(const BackItem* items, int n, int64_t blocks,       \
+                                   int dlen_kind, int pen, int fh, int comp,            \
+                                   cudaStream_t st) {                                   \
+    back_multi<KK>(items, n, blocks, dlen_kind, pen, fh, comp, st);                     \
   }
 
 }  // namespace tg

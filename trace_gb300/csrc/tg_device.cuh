@@ -223,12 +223,21 @@ __device__ __forceinline__ float u16_to_float(uint32_t q) {
   return __uint_as_float(0x4B000000u | q) - 8388608.0f;
 }
 
-// Backward-matrix position of pixel (x, y): 8x4 pixel tiles, one warp per
-// tile, tiles row-major; entry (angle, tile, lane) is one 32-lane row.
-__device__ __forceinline__ void pixel_tile(int x, int y, int tiles_x, int* tile,
-                                           int* lane) {
-  *tile = (y >> 2) * tiles_x + (x >> 3);
-  *lane = ((y & 3) << 3) | (x & 7);
+// Backward-matrix position of pixel (x, y): tiles of 32 pixels, 2^tw_shift
+// wide and 2^(5 - tw_shift) high (16x2, 8x4 or 4x8), one warp per tile,
+// tiles row-major; entry (angle, tile, lane) is one 32-lane row.
+__device__ __forceinline__ void pixel_tile(int x, int y, int tiles_x, int tw_shift,
+                                           int* tile, int* lane) {
+  const int th_shift = 5 - tw_shift;
+  *tile = (y >> th_shift) * tiles_x + (x >> tw_shift);
+  *lane = ((y & ((1 << th_shift) - 1)) << tw_shift) | (x & ((1 << tw_shift) - 1));
+}
+
+// The pixel of lane `lane` in tile `tile` (inverse of pixel_tile).
+__device__ __forceinline__ void tile_pixel(int tile, int lane, int tiles_x, int tw_shift,
+                                           int* x, int* y) {
+  *x = ((tile % tiles_x) << tw_shift) + (lane & ((1 << tw_shift) - 1));
+  *y = ((tile / tiles_x) << (5 - tw_shift)) + (lane >> tw_shift);
 }
 
 // ---- segment-length storage -------------------------------------------------

@@ -45,8 +45,8 @@ __global__ void k_weights64(DevGeom G, MatrixDev M, double* W) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)M.ntiles * 32) return;
   const int tile = (int)(t >> 5), lane = (int)(t & 31);
-  const int x = (tile % M.tiles_x) * 8 + (lane & 7);
-  const int y = (tile / M.tiles_x) * 4 + (lane >> 3);
+  int x, y;
+  tile_pixel(tile, lane, M.tiles_x, M.tw_shift, &x, &y);
   if (x >= g || y >= g) return;
   const float2* d = reinterpret_cast<const float2*>(M.dlen);
   double sum = 0.0;
@@ -69,8 +69,8 @@ __global__ void __launch_bounds__(kBlock)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tile = blockIdx.x * 8 + warp;
   if (tile >= A.M.ntiles) return;
-  const int x = (tile % A.M.tiles_x) * 8 + (lane & 7);
-  const int y = (tile / A.M.tiles_x) * 4 + (lane >> 3);
+  int x, y;
+  tile_pixel(tile, lane, A.M.tiles_x, A.M.tw_shift, &x, &y);
   if (x >= g || y >= g) return;
   const int64_t p = (int64_t)y * g + x;
   const bool pen = A.alg >= 2;

@@ -22,18 +22,20 @@ struct MatrixDev {
   const int* rstart;      // delta form: [P*C] first pixel of each ray
   const void* rlen;    // length per entry (float or 16-bit code)
   const float* ra2;    // [P*C] sum of squared lengths (SIRT's a2)
-  // backward matrix, angle-major over 8x4 pixel tiles: for pixel (x, y) in
-  // tile t at lane l, dlen[((a*ntiles + t)*32 + l)*2 + slot] is the length of
-  // ray (a, window_c0 + slot) through the pixel
+  // backward matrix, angle-major over 32-pixel tiles (pixel_tile: 16x2, 8x4
+  // or 4x8 pixels): for pixel (x, y) in tile t at lane l, the pair of angle a
+  // at dense_pair(ntiles, a, t, l) holds the lengths of rays (a, window_c0)
+  // and (a, window_c0 + 1) through the pixel
   const void* dlen;
   const float4* wcoef; // [P4] window coefficients {-sin, cos, D, 0}
   // segments outside their pixel's two-column window (rare: the reference's
   // tracer puts a stray segment far from its ray at some near-vertical
-  // angles): per 8x4 tile t, entries exc[exc_first[t] .. exc_first[t+1]) =
+  // angles): per pixel tile t, entries exc[exc_first[t] .. exc_first[t+1]) =
   // {lane, angle, column, length bits}; exc_first == nullptr when none
   const int* exc_first;
   const int4* exc;
   int tiles_x, ntiles;
+  int tw_shift;        // backward tiles are 2^tw_shift pixels wide
   int P4;              // angles rounded up to a multiple of 4 (padding empty)
   const float* W;      // [g*g] total length through each pixel
   const float* Wh;     // [g*g] the same over half-rounded lengths (half_gathers)
@@ -44,12 +46,14 @@ struct MatrixDev {
   float scale, inv_scale;
 };
 
-// Tile-staged forward matrix (tg_tiles.cu): per 64x64 tile, groups of 32
-// runs (consecutive segments of one ray inside the tile), lane = run.
+// Tile-staged forward matrix (tg_tiles.cu): per ts x ts tile, groups of 32
+// runs (consecutive segments of one ray inside the tile), lane = run. The
+// tile side ts is a plan choice (32, 64 or 96; a step inside a tile is one
+// signed byte dx + dy * (ts + 1), so ts + 1 <= 127).
 constexpr int kTileSide = 64;
 
-__device__ __forceinline__ int tile_of_pixel(int ix, int iy, int tiles_x) {
-  return (iy / kTileSide) * tiles_x + ix / kTileSide;
+__device__ __forceinline__ int tile_of_pixel(int ix, int iy, int tiles_x, int ts) {
+  return (iy / ts) * tiles_x + ix / ts;
 }
 
 // A 4-bit step code holds (dx, dy) in {0,1} x {-1,0,1}. The reference's
@@ -68,6 +72,7 @@ __device__ __forceinline__ bool unit_step(int ix, int iy, int px, int py) {
 // runs in path order. No atomics: the forward projection is bit-reproducible.
 struct TileMatrixDev {
   int tiles_x, ntiles;
+  int ts;                   // tile side (pixels); shared-memory row stride ts + 1
   const int* group_first;   // [ntiles + 1] first group of each tile
   const int* gpart;         // [groups * 32] partial-sum slot of each lane's
                             // run, -1 if the lane is empty
@@ -114,6 +119,50 @@ struct IterArgs {
   int comp;
 };
 
+// Work items of the launches that serve many plans at once (tg_batch): one
+// item is one plan's slice batch, `first` its first block in the launch
+// (items ascending by it).
+struct FwdItem {
+  TileMatrixDev T;
+  const float* recon;   // the batch's reconstruction slots
+  float* part;          // the plan's partial-sum slots
+  int g;
+  float inv_scale;
+  int64_t first;
+};
+struct FinItem {
+  const int* rnrun;
+  const int* pbase;
+  const float* ra2;
+  const float* part;
+  const float* sino;    // the batch's sinogram rows
+  float* out;           // per-ray factors
+  int64_t nrays;
+  int64_t first;        // 256 rays a block
+  int out_mode;
+  int fh;               // factors stored as halves of (factor - 1)
+};
+struct BackItem {
+  IterArgs A;
+  int batch;
+  const float* cur;
+  float* next;
+  const float* upd;
+  int64_t first;
+};
+
+// The item a block belongs to.
+template <class Item>
+__device__ __forceinline__ int item_of(const Item* items, int n, int64_t block) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (items[mid].first <= block) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // Address of (slot, pixel) in the batched reconstruction layout.
 __device__ __forceinline__ int64_t slot_addr(int slot, int64_t p, int64_t g2,
                                              int K) {
@@ -137,7 +186,7 @@ __device__ __forceinline__ void apmlr_axial(const IterArgs& A, int s, int* up,
 // ray_nruns (optional): runs per ray of the tile-ordered forward matrix
 // (a new run at each tile change and non-unit step), counted in the same pass
 void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
-                        unsigned* maxlen_bits, int tiles_x, int* ray_nruns,
+                        unsigned* maxlen_bits, int tiles_x, int ts, int* ray_nruns,
                         cudaStream_t st);
 void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
                        uint32_t* rcode, int* rstart, void* rlen, float* ra2,
@@ -171,7 +220,10 @@ void launch_forward(const IterArgs& A, const float* recon_batch,
 #define TG_BACKWARD_DECL(KK)                                                      \
   void launch_backward_k##KK(const IterArgs& A, int batch, const float* recon_cur, \
                              float* recon_next, const float* upd, float* rep_num, \
-                             int epi, cudaStream_t st);
+                             int epi, cudaStream_t st);                            \
+  void launch_backward_multi_k##KK(const BackItem* items, int n, int64_t blocks,   \
+                                   int dlen_kind, int pen, int fh, int comp,        \
+                                   cudaStream_t st);
 TG_BACKWARD_DECL(1)
 TG_BACKWARD_DECL(2)
 TG_BACKWARD_DECL(4)
@@ -206,21 +258,22 @@ struct RunKey {
 };
 // Run emission and the tile-stream fill read each ray's segments back from
 // the ray-ordered forward matrix M when it is stored (M.rlen), else trace them.
-void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, RunKey rk,
+void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts, RunKey rk,
                       const int64_t* ray_run_off, unsigned long long* key, int* val,
                       uint16_t* run_lp, uint16_t* run_len, int* tile_count,
                       cudaStream_t st);
 int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
               int* val_in, int* val_out, int64_t n, int end_bit,
               cudaStream_t st);
+// lanes of each 32-run group, dealt by the bank group of the runs' start
+// pixels in the shared-memory tile (bpp: bytes per pixel of one load)
 void launch_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
-                       int64_t nruns, const int* tile_first_run,
+                       int ntiles, int64_t ngroups, const int* tile_first_run,
                        const int* group_first, const uint16_t* run_lp,
                        const uint16_t* run_len, const int64_t* ray_run_off,
-                       const int* pbase, int* gpart, uint16_t* glp,
-                       uint16_t* glen, int* gsteps, int* run_slot,
-                       cudaStream_t st);
-void launch_runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x,
+                       const int* pbase, int ts, int bpp, int* gpart, uint16_t* glp,
+                       uint16_t* glen, int* gsteps, int* run_slot, cudaStream_t st);
+void launch_runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts,
                       const int64_t* ray_run_off, const int* run_slot,
                       const int64_t* gseg_off, const int64_t* gcode_off,
                       void* tlen, uint32_t* tcode, cudaStream_t st);
@@ -230,6 +283,20 @@ void launch_forward_tiled(const IterArgs& A, const TileMatrixDev& T,
 // ray sums from the partial sums (fixed order) -> per-ray values `out`
 void launch_fwd_finish(const IterArgs& A, const TileMatrixDev& T, const float* part,
                        const float* sino, float* out, int out_mode, cudaStream_t st);
+// the same over many plans' slice batches in one launch each (device item
+// arrays; blocks = the launch's total blocks; all items of one launch share
+// K, the tile side and precision and the summation; 16-bit fixed-point
+// lengths)
+void launch_forward_tiled_multi(const FwdItem* items, int n, int64_t blocks, int K, int ts,
+                                int half_tile, int comp, cudaStream_t st);
+void launch_fwd_finish_multi(const FinItem* items, int n, int64_t blocks, int K, int comp,
+                             cudaStream_t st);
+// plans with 16-bit fixed-point lengths (backward matrix u16, or f16 with
+// half gathers); pen: PML/APMLR; fh: half factors
+void launch_backward_multi(const BackItem* items, int n, int64_t blocks, int K,
+                           int dlen_kind, int pen, int fh, int comp, cudaStream_t st);
+// blocks (of 256 threads) a plan's backprojection launch uses
+int64_t backward_blocks(const IterArgs& A);
 // tg_iter.cu
 void launch_fg(const IterArgs& A, const float* recon, const float* W, float* F,
                float* Gv, cudaStream_t st);

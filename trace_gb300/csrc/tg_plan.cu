@@ -2,6 +2,7 @@
 // (geometry tables, tracing, matrix construction), state upload/download,
 // and the per-iteration launch sequence.
 #include <algorithm>
+#include <map>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -17,6 +18,7 @@ using namespace tg;
 struct tg_plan {
   tg_plan_desc d{};
   int C = 0, P = 0, S = 0, K = 1;
+  int fts = kTileSide;  // forward tile side (forward_tiles)
   int64_t g2 = 0, R = 0;
   float mov = 0.f;
   int len_kind = 0;
@@ -35,7 +37,7 @@ struct tg_plan {
   void* d_dlen = nullptr;
   float* d_W = nullptr;
   float* d_Wh = nullptr;  // half_gathers: total of the half-rounded lengths
-  int* d_exc_first = nullptr;  // window exceptions (CSR over 8x4 tiles)
+  int* d_exc_first = nullptr;  // window exceptions (CSR over the pixel tiles)
   int4* d_exc = nullptr;
   // tile-staged forward (fast mode): the tile-ordered matrix + the runs'
   // partial sums ([runs][K], one slot per run)
@@ -305,7 +307,7 @@ float* batch_ptr(tg_plan* p, float* base, int batch_slot) {
 int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
   const DevGeom& G = p->G;
   const int C = p->C;
-  const int tiles_x = (C + kTileSide - 1) / kTileSide;
+  const int tiles_x = (C + p->fts - 1) / p->fts;
   const int ntiles = tiles_x * tiles_x;
   int tile_bits = 1;
   while ((1 << tile_bits) < ntiles) ++tile_bits;
@@ -343,7 +345,7 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
       (rc = talloc(&tile_count, (size_t)ntiles, true)))
     return release(), rc;
   cudaMemcpyAsync(d_run_off, run_off.data(), p->R * 8, cudaMemcpyHostToDevice, p->st);
-  launch_runs_emit(G, p->M, tiles_x, rk, d_run_off, key, val, run_lp, run_len, tile_count,
+  launch_runs_emit(G, p->M, tiles_x, p->fts, rk, d_run_off, key, val, run_lp, run_len, tile_count,
                    p->st);
   if (sort_runs(key, key2, val, val2, NR, end_bit, p->st))
     return release(), fail(p, TG_E_CUDA, "sorting the tile runs failed");
@@ -390,9 +392,13 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
   cudaMemcpyAsync(d_group_first, group_first.data(), (ntiles + 1) * 4, cudaMemcpyHostToDevice, p->st);
   cudaMemcpyAsync(rnrun, nruns.data(), p->R * 4, cudaMemcpyHostToDevice, p->st);
   cudaMemcpyAsync(pbase, pbase_h.data(), rgroups * 4, cudaMemcpyHostToDevice, p->st);
-  launch_runs_group(rk, key2, val2, NR, d_tile_first, d_group_first, run_lp, run_len,
-                    d_run_off, pbase, gpart,
-                    glp, glen, gsteps, run_slot, p->st);
+  // bytes per pixel of one shared-memory load in the forward: K halves (half
+  // tile), or a plane of up to 4 floats
+  const bool half_tile = p->d.half_gathers || p->K == 16;
+  const int bpp = half_tile ? 2 * p->K : 4 * std::min(p->K, 4);
+  launch_runs_group(rk, key2, val2, ntiles, groups, d_tile_first, d_group_first, run_lp,
+                    run_len, d_run_off, pbase, p->fts, bpp, gpart, glp, glen, gsteps,
+                    run_slot, p->st);
   std::vector<int> steps(groups);
   cudaMemcpyAsync(steps.data(), gsteps, (size_t)groups * 4, cudaMemcpyDeviceToHost, p->st);
   if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run grouping failed");
@@ -423,7 +429,7 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
   }
   cudaMemcpyAsync(d_seg_off, seg_off.data(), groups * 8, cudaMemcpyHostToDevice, p->st);
   cudaMemcpyAsync(d_code_off, code_off.data(), groups * 8, cudaMemcpyHostToDevice, p->st);
-  launch_runs_fill(G, p->M, tiles_x, d_run_off, run_slot, d_seg_off, d_code_off, tlen,
+  launch_runs_fill(G, p->M, tiles_x, p->fts, d_run_off, run_slot, d_seg_off, d_code_off, tlen,
                    tcode, p->st);
   if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run fill failed");
   release();
@@ -431,6 +437,7 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
   TileMatrixDev& T = p->T;
   T.tiles_x = tiles_x;
   T.ntiles = ntiles;
+  T.ts = p->fts;
   T.group_first = d_group_first;
   T.gpart = gpart;
   T.rnrun = rnrun;
@@ -513,9 +520,31 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
       (d.len_storage != TG_LEN_F32 || d.slices_per_pass != 1 || d.delta_index))
     return fail(nullptr, TG_E_ARG,
                 "FP64 mode needs f32 lengths, explicit indices and one slice per pass");
-  if (d.compensated && (d.mode != TG_MODE_FAST || !d.forward_tiles || d.backward_staged))
+  if (d.compensated && (d.mode != TG_MODE_FAST || !d.forward_tiles || d.backward_staged ||
+                        d.slices_per_pass > 8))
     return fail(nullptr, TG_E_ARG,
-                "compensated needs fast mode, forward_tiles and the L1 backprojection");
+                "compensated needs fast mode, forward_tiles, the L1 backprojection and "
+                "at most 8 slices per pass");
+  if (d.forward_tile_side != 0 && d.forward_tile_side != 32 && d.forward_tile_side != 64 &&
+      d.forward_tile_side != 96)
+    return fail(nullptr, TG_E_ARG, "forward_tile_side must be 0, 32, 64 or 96");
+  if (d.forward_tiles) {
+    // the shared-memory tile: side x (side + 1) pixels of slices_per_pass
+    // values, halves with half_gathers (and always at 16 slices per pass)
+    const int64_t ts = d.forward_tile_side ? d.forward_tile_side : kTileSide;
+    const int64_t bytes = ts * (ts + 1) * d.slices_per_pass *
+                          ((d.half_gathers || d.slices_per_pass == 16) ? 2 : 4);
+    if (bytes > 232448)
+      return fail(nullptr, TG_E_ARG,
+                  "the forward tile (" + std::to_string(bytes) +
+                      " bytes) does not fit shared memory; use a smaller "
+                      "forward_tile_side, fewer slices per pass or half_gathers");
+  }
+  if (d.backward_tile_width != 0 && d.backward_tile_width != 4 &&
+      d.backward_tile_width != 8 && d.backward_tile_width != 16)
+    return fail(nullptr, TG_E_ARG, "backward_tile_width must be 0, 4, 8 or 16");
+  if (d.backward_staged && d.backward_tile_width != 0 && d.backward_tile_width != 8)
+    return fail(nullptr, TG_E_ARG, "backward_staged uses 8x4 pixel tiles");
   if ((sin_tab == nullptr) != (cos_tab == nullptr))
     return fail(nullptr, TG_E_ARG, "give both sin_tab and cos_tab or neither");
 
@@ -532,6 +561,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   p->len_kind = d.len_storage;
   p->nb = (p->S + p->K - 1) / p->K;
   p->fp64 = d.mode == TG_MODE_FP64;
+  if (d.forward_tile_side) p->fts = d.forward_tile_side;
 
   auto bail = [&](int rc) {
     g_create_error = p->err;
@@ -600,7 +630,10 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   if ((rc = dalloc(p, &p->d_wcoef, P4))) return bail(rc);
   cudaMemcpyAsync(p->d_wcoef, wc.data(), P4 * sizeof(float4),
                   cudaMemcpyHostToDevice, p->st);
-  const int tiles_x = (C + 7) / 8, tiles_y = (C + 3) / 4;
+  // backward pixel tiles: 2^tw_shift x 2^(5 - tw_shift)
+  const int tw = d.backward_tile_width ? d.backward_tile_width : 8;
+  const int tw_shift = tw == 16 ? 4 : tw == 4 ? 2 : 3;
+  const int tiles_x = (C + tw - 1) / tw, tiles_y = (C + (32 / tw) - 1) / (32 / tw);
 
   // pass 1: segment counts, per-group capacity, longest segment
   const int ngroups = P * G.gpa;
@@ -616,8 +649,8 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     if ((rc = dalloc(p, &d_nruns, (size_t)p->R))) return bail(rc);
     h_nruns.resize(p->R);
   }
-  launch_trace_count(G, p->d_rnseg, p->d_rcap, p->d_maxlen,
-                     (C + kTileSide - 1) / kTileSide, d_nruns, p->st);
+  launch_trace_count(G, p->d_rnseg, p->d_rcap, p->d_maxlen, (C + p->fts - 1) / p->fts,
+                     p->fts, d_nruns, p->st);
   if (d_nruns)
     cudaMemcpyAsync(h_nruns.data(), d_nruns, p->R * 4, cudaMemcpyDeviceToHost, p->st);
   std::vector<int> rcap(ngroups);
@@ -704,6 +737,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   M.wcoef = p->d_wcoef;
   M.tiles_x = tiles_x;
   M.ntiles = tiles_x * tiles_y;
+  M.tw_shift = tw_shift;
   M.P4 = P4;
   M.W = p->d_W;
   M.Wh = p->d_Wh;
@@ -740,7 +774,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     return bail(TG_E_GEOMETRY);
   }
   if (nexc > 0) {
-    // window exceptions as a CSR list over the 8x4 pixel tiles
+    // window exceptions as a CSR list over the pixel tiles
     std::vector<int4> ex(nexc);
     std::vector<int> et(nexc);
     cudaMemcpy(ex.data(), d_exc_tmp, nexc * sizeof(int4), cudaMemcpyDeviceToHost);
@@ -1146,7 +1180,238 @@ struct tg_batch {
     cudaGraphExec_t exec = nullptr;
   } graphs[2];
   std::string err;
+  // Multi-plan launches (every plan fast mode, tile-staged forward, L1
+  // backprojection, 16-bit fixed-point lengths): one iteration of all plans
+  // is, per slice batch round, one launch per kernel variant whose blocks
+  // walk the work items of every plan. Each iteration state (the plans'
+  // buffer parities and factor precisions) has its device work items and a
+  // CUDA graph of its launches.
+  bool multi = false;
+  int last_launches = 0;  // kernel launches per iteration, last tg_batch_iterate
+  struct State {
+    std::string key;
+    void* d_items = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int launches = 0;
+  };
+  std::vector<State> states;
 };
+
+namespace {
+
+bool multi_eligible(const tg_plan* p) {
+  return !p->fp64 && p->tiles && !p->d.backward_staged && p->d.mode == TG_MODE_FAST &&
+         p->len_kind == TG_LEN_U16;
+}
+
+void drop_states(tg_batch* b) {
+  for (auto& s : b->states) {
+    if (s.exec) cudaGraphExecDestroy(s.exec);
+    if (s.d_items) cudaFree(s.d_items);
+  }
+  b->states.clear();
+}
+
+// A launch of the multi-plan kernels: kind 0 forward, 1 finish, 2 backward;
+// its items start at byte `off` of the state's item buffer.
+struct MultiLaunch {
+  int kind, branch, K, ts, half_tile, comp, dlen, pen, fh;
+  size_t off;
+  int n;
+  int64_t blocks;
+};
+
+// Key of iteration `it` (counted from now) of the batch: algorithms,
+// parameters and every plan's buffer parity and factor precision then.
+std::string multi_key(const tg_batch* b, const int* algs, const tg_params* params, int it) {
+  std::string k;
+  for (size_t i = 0; i < b->plans.size(); ++i) {
+    const tg_plan* p = b->plans[i];
+    const int mode = algs[i] == TG_SIRT ? FWD_SIRT : FWD_RATIO;
+    const int cur = p->cur ^ (it & 1);
+    const int hf = p->tiles && p->d.half_gathers && mode == FWD_RATIO && p->iters_done + it >= 1;
+    const tg_params prm = params ? params[i] : tg_params{};
+    k.append(reinterpret_cast<const char*>(&algs[i]), sizeof(int));
+    k.append(reinterpret_cast<const char*>(&prm), sizeof(prm));
+    k.push_back((char)(cur | (hf << 1)));
+  }
+  return k;
+}
+
+// Work items and launches of one iteration state. Plans are split into
+// branches by the forward kernel they take (slices per pass, tile side and
+// precision, summation); a branch's launches form one chain - per round of
+// slice batches a forward launch, a finish launch and one backprojection
+// launch per (penalty, factor precision) - and branches share no plan, so
+// they run concurrently.
+void multi_build(const tg_batch* b, const int* algs, const tg_params* params, int it,
+                 std::vector<char>& bytes, std::vector<MultiLaunch>& launches) {
+  auto put = [&](const void* src, size_t n) {
+    const size_t off = (bytes.size() + 15) / 16 * 16;
+    bytes.resize(off + n);
+    std::memcpy(bytes.data() + off, src, n);
+    return off;
+  };
+  std::map<std::vector<int>, std::vector<int>> branches;  // key -> plan indices
+  for (size_t i = 0; i < b->plans.size(); ++i) {
+    const tg_plan* p = b->plans[i];
+    const int half_tile = p->K == 16 || p->d.half_gathers;
+    branches[{p->K, p->T.ts, half_tile, p->d.compensated}].push_back((int)i);
+  }
+  int branch = 0;
+  for (auto& br : branches) {
+    const std::vector<int>& key = br.first;
+    int rounds = 0;
+    for (int i : br.second) rounds = std::max(rounds, b->plans[i]->nb);
+    for (int r = 0; r < rounds; ++r) {
+      std::vector<FwdItem> fwd;
+      std::vector<FinItem> fin;
+      std::map<std::vector<int>, std::vector<BackItem>> back;
+      for (int i : br.second) {
+        tg_plan* p = b->plans[i];
+        if (r >= p->nb) continue;
+        const int mode = algs[i] == TG_SIRT ? FWD_SIRT : FWD_RATIO;
+        const int cur = p->cur ^ (it & 1);
+        const int hf = p->d.half_gathers && mode == FWD_RATIO && p->iters_done + it >= 1;
+        IterArgs A = make_args(p, algs[i], params ? &params[i] : nullptr);
+        A.half_tile = p->d.half_gathers;
+        A.half_factors = hf;
+        FwdItem f{};
+        f.T = p->T;
+        f.recon = batch_ptr(p, p->d_recon[cur], r * p->K + p->fshift);
+        f.part = p->d_part;
+        f.g = p->C;
+        f.inv_scale = A.M.inv_scale;
+        f.first = p->T.ntiles;  // block count; turned into offsets below
+        fwd.push_back(f);
+        FinItem n{};
+        n.rnrun = p->T.rnrun;
+        n.pbase = p->T.pbase;
+        n.ra2 = A.M.ra2;
+        n.part = p->d_part;
+        n.sino = p->d_sino + (int64_t)r * p->R * p->K;
+        n.out = p->d_upd;
+        n.nrays = p->R;
+        n.first = (p->R + 255) / 256;
+        n.out_mode = mode;
+        n.fh = hf;
+        fin.push_back(n);
+        BackItem k{};
+        k.A = A;
+        k.batch = r;
+        k.cur = p->d_recon[cur];
+        k.next = p->d_recon[cur ^ 1];
+        k.upd = p->d_upd;
+        k.first = backward_blocks(A);
+        back[{A.M.dlen_kind, algs[i] >= TG_PML, hf}].push_back(k);
+      }
+      auto emit = [&](int kind, auto& items, int dlen, int pen, int fh) {
+        int64_t total = 0;
+        for (auto& x : items) {
+          const int64_t nb = x.first;
+          x.first = total;
+          total += nb;
+        }
+        MultiLaunch l{};
+        l.kind = kind;
+        l.branch = branch;
+        l.K = key[0];
+        l.ts = key[1];
+        l.half_tile = key[2];
+        l.comp = key[3];
+        l.dlen = dlen;
+        l.pen = pen;
+        l.fh = fh;
+        l.off = put(items.data(), items.size() * sizeof(items[0]));
+        l.n = (int)items.size();
+        l.blocks = total;
+        launches.push_back(l);
+      };
+      emit(0, fwd, 0, 0, 0);
+      emit(1, fin, 0, 0, 0);
+      for (auto& c : back) emit(2, c.second, c.first[0], c.first[1], c.first[2]);
+    }
+    ++branch;
+  }
+}
+
+// Issues the launches, branch k on stream branch_st[k % n] (forked from and
+// joined back into `st` by the caller).
+void multi_issue(const std::vector<MultiLaunch>& launches, const char* d_items,
+                 const std::vector<cudaStream_t>& branch_st) {
+  for (const MultiLaunch& l : launches) {
+    const void* items = d_items + l.off;
+    const cudaStream_t st = branch_st[l.branch % branch_st.size()];
+    if (l.kind == 0)
+      launch_forward_tiled_multi(static_cast<const FwdItem*>(items), l.n, l.blocks, l.K,
+                                 l.ts, l.half_tile, l.comp, st);
+    else if (l.kind == 1)
+      launch_fwd_finish_multi(static_cast<const FinItem*>(items), l.n, l.blocks, l.K, l.comp,
+                              st);
+    else
+      launch_backward_multi(static_cast<const BackItem*>(items), l.n, l.blocks, l.K, l.dlen,
+                            l.pen, l.fh, l.comp, st);
+  }
+}
+
+// The state of iteration `it`, built (items uploaded, launches captured)
+// when it is new. Keeps the most recent few.
+int multi_state(tg_batch* b, const int* algs, const tg_params* params, int it,
+                tg_batch::State** out) {
+  const std::string key = multi_key(b, algs, params, it);
+  for (auto& s : b->states)
+    if (s.key == key) {
+      *out = &s;
+      return TG_OK;
+    }
+  if (b->states.size() >= 6) {
+    cudaStreamSynchronize(b->main);
+    if (b->states.front().exec) cudaGraphExecDestroy(b->states.front().exec);
+    if (b->states.front().d_items) cudaFree(b->states.front().d_items);
+    b->states.erase(b->states.begin());
+  }
+  std::vector<char> bytes;
+  std::vector<MultiLaunch> launches;
+  multi_build(b, algs, params, it, bytes, launches);
+  tg_batch::State s;
+  s.key = key;
+  s.launches = (int)launches.size();
+  cudaError_t e = cudaMalloc(&s.d_items, std::max<size_t>(bytes.size(), 16));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(s.d_items, bytes.data(), bytes.size(), cudaMemcpyHostToDevice);
+  cudaGraph_t graph = nullptr;
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    // fork the branch streams from `main`, issue, join them back
+    int nbranch = 0;
+    for (const MultiLaunch& l : launches) nbranch = std::max(nbranch, l.branch + 1);
+    const int ns = std::min<int>(nbranch, (int)b->streams.size());
+    std::vector<cudaStream_t> bst(b->streams.begin(), b->streams.begin() + std::max(ns, 1));
+    cudaError_t ef = cudaEventRecord(b->fork, b->main);
+    for (int k = 0; ef == cudaSuccess && k < ns; ++k)
+      ef = cudaStreamWaitEvent(bst[k], b->fork, 0);
+    if (ef == cudaSuccess) multi_issue(launches, static_cast<const char*>(s.d_items), bst);
+    for (int k = 0; ef == cudaSuccess && k < ns; ++k) {
+      ef = cudaEventRecord(b->joins[k], bst[k]);
+      if (ef == cudaSuccess) ef = cudaStreamWaitEvent(b->main, b->joins[k], 0);
+    }
+    const cudaError_t e1 = ef != cudaSuccess ? ef : cudaGetLastError();
+    const cudaError_t e2 = cudaStreamEndCapture(b->main, &graph);
+    e = e1 != cudaSuccess ? e1 : e2;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&s.exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    if (s.d_items) cudaFree(s.d_items);
+    b->err = std::string("multi-plan iteration setup failed: ") + cudaGetErrorString(e);
+    return TG_E_CUDA;
+  }
+  b->states.push_back(s);
+  *out = &b->states.back();
+  return TG_OK;
+}
+
+}  // namespace
 
 extern "C" int tg_batch_create(tg_plan* const* plans, int n, tg_batch** out) {
   if (!plans || n < 1 || !out) return fail(nullptr, TG_E_ARG, "need plans");
@@ -1157,6 +1422,8 @@ extern "C" int tg_batch_create(tg_plan* const* plans, int n, tg_batch** out) {
   tg_batch* b = new (std::nothrow) tg_batch();
   if (!b) return fail(nullptr, TG_E_NOMEM, "host allocation failed");
   b->plans.assign(plans, plans + n);
+  b->multi = true;
+  for (int i = 0; i < n; ++i) b->multi = b->multi && multi_eligible(plans[i]);
   const int nstreams = n < 16 ? n : 16;
   bool ok = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
@@ -1182,6 +1449,7 @@ extern "C" int tg_batch_create(tg_plan* const* plans, int n, tg_batch** out) {
 extern "C" int tg_batch_destroy(tg_batch* b) {
   if (!b) return TG_OK;
   if (b->main) cudaStreamSynchronize(b->main);
+  drop_states(b);
   for (auto& g : b->graphs)
     if (g.exec) cudaGraphExecDestroy(g.exec);
   for (auto s : b->streams) cudaStreamDestroy(s);
@@ -1189,6 +1457,13 @@ extern "C" int tg_batch_destroy(tg_batch* b) {
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->main) cudaStreamDestroy(b->main);
   delete b;
+  return TG_OK;
+}
+
+extern "C" int tg_batch_get_info(const tg_batch* b, int* multi, int* launches) {
+  if (!b) return TG_E_ARG;
+  if (multi) *multi = b->multi ? 1 : 0;
+  if (launches) *launches = b->last_launches;
   return TG_OK;
 }
 
@@ -1224,6 +1499,31 @@ extern "C" int tg_batch_iterate(tg_batch* b, const int* algs, const tg_params* p
   }
   // plans' own streams must be done before the graph (on `main`) reads their data
   for (tg_plan* p : b->plans) cudaStreamSynchronize(p->st);
+  if (b->multi) {
+    for (int it = 0; it < n_iter; ++it) {
+      tg_batch::State* s = nullptr;
+      const int rc = multi_state(b, algs, params, 0, &s);
+      if (rc) return rc;
+      b->last_launches = s->launches;
+      const cudaError_t e = cudaGraphLaunch(s->exec, b->main);
+      if (e != cudaSuccess) {
+        b->err = cudaGetErrorString(e);
+        return TG_E_CUDA;
+      }
+      for (tg_plan* p : b->plans) {
+        p->cur ^= 1;
+        ++p->iters_done;
+      }
+    }
+    const cudaError_t e = cudaStreamSynchronize(b->main);
+    if (e != cudaSuccess) {
+      b->err = cudaGetErrorString(e);
+      return TG_E_CUDA;
+    }
+    return TG_OK;
+  }
+  b->last_launches = 0;
+  for (tg_plan* p : b->plans) b->last_launches += p->nb * (p->tiles ? 3 : 2);
   for (int it = 0; it < n_iter; ++it) {
     const int parity = b->plans[0]->cur;
     tg_batch::Graph& g = b->graphs[parity];

@@ -33,19 +33,20 @@ namespace tg {
 
 namespace {
 
-constexpr int TS = kTileSide;     // tile side (pixels)
-constexpr int RS = TS + 1;        // shared-memory row stride (bank spread)
 constexpr int kBlock = 1024;      // forward: 32 warps per tile
 constexpr int kTraceBlock = 128;
-// A step is stored as the signed byte dx + dy * RS, the change of the
-// shared-memory pixel index (dx in {0, 1}, dy in {-1, 0, 1}: -65 .. 66), so
+// Tiles are ts x ts pixels (TileMatrixDev::ts), kept in shared memory with
+// row stride ts + 1 (bank spread).
+// A step is stored as the signed byte dx + dy * (ts + 1), the change of the
+// shared-memory pixel index (dx in {0, 1}, dy in {-1, 0, 1}: -97 .. 98 at
+// the largest tile side, 96), so
 // the forward walks a run with one byte extraction and one add per step.
 // 0 is "stay", never a real step: every unused byte of the stream (a run's
 // first step, steps past a run's end, empty lanes) holds it, with a zero
 // length. Per lane and chunk the 8 bytes are one 8-byte word pair.
 
-__device__ __forceinline__ int tile_of(const DevGeom&, int ix, int iy, int tiles_x) {
-  return tile_of_pixel(ix, iy, tiles_x);
+__device__ __forceinline__ int tile_of(int ix, int iy, int tiles_x, int ts) {
+  return tile_of_pixel(ix, iy, tiles_x, ts);
 }
 
 // ---- construction (runs per ray are counted by k_trace_count) ----------------
@@ -114,7 +115,7 @@ __device__ __forceinline__ unsigned long long run_key(RunKey rk, int t, int len,
 
 template <int SRC>
 __global__ void __launch_bounds__(kTraceBlock)
-    k_runs_emit(DevGeom G, MatrixDev M, int tiles_x, RunKey rk,
+    k_runs_emit(DevGeom G, MatrixDev M, int tiles_x, int ts, RunKey rk,
                 const int64_t* ray_run_off, unsigned long long* key, int* val,
                 uint16_t* run_lp, uint16_t* run_len, int* tile_count) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -128,7 +129,7 @@ __global__ void __launch_bounds__(kTraceBlock)
     }
   };
   ray_segments<SRC, false>(G, M, r, [&](int, int ix, int iy, float, uint16_t) {
-    const int t = tile_of(G, ix, iy, tiles_x);
+    const int t = tile_of(ix, iy, tiles_x, ts);
     const bool step_ok = unit_step(ix, iy, px, py);
     px = ix;
     py = iy;
@@ -139,7 +140,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       cur = t;
       len = 0;
       val[i] = (int)i;
-      run_lp[i] = (uint16_t)((iy % TS) * TS + ix % TS);
+      run_lp[i] = (uint16_t)((iy % ts) * ts + ix % ts);
       atomicAdd(&tile_count[t], 1);
     }
     ++len;
@@ -147,36 +148,75 @@ __global__ void __launch_bounds__(kTraceBlock)
   close();
 }
 
+// One warp per group: the group's 32 runs (consecutive in the sorted order
+// of their tile) get their lanes. The forward reads one pixel per lane and
+// step from the shared-memory tile; lanes of one load phase (8 lanes for a
+// 16-byte load) collide when their pixels fall in the same 16-byte bank
+// group. The runs of a group are adjacent parallel rays that step through
+// the tile nearly in lockstep, their entry points up to sqrt(2) pixels apart
+// along an edge, so consecutive runs can wrap onto the same bank group.
+// Lanes are therefore dealt by the bank group of each run's start pixel:
+// runs sorted by (bank group, rank) go round-robin over the load phases.
+// bpp: bytes per pixel of one shared-memory load (16 for 8 halves or a
+// 4-float plane, 32 for 16 halves, 8 / 4 for fewer slices).
 __global__ void k_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
-                             int64_t nruns, const int* tile_first_run,
+                             int ntiles, int64_t ngroups, const int* tile_first_run,
                              const int* group_first, const uint16_t* run_lp,
                              const uint16_t* run_len, const int64_t* ray_run_off,
-                             const int* pbase, int* gpart, uint16_t* glp,
+                             const int* pbase, int ts, int bpp, int* gpart, uint16_t* glp,
                              uint16_t* glen, int* gsteps, int* run_slot) {
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nruns) return;
+  const int64_t grp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (grp >= ngroups) return;  // whole warps
+  // the group's tile: the last t with group_first[t] <= grp
+  int lo = 0, hi = ntiles - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (group_first[mid] <= grp) lo = mid;
+    else hi = mid - 1;
+  }
+  const int t = lo;
+  const int rank = (int)(grp - group_first[t]) * 32 + lane;
+  const bool valid = rank < tile_first_run[t + 1] - tile_first_run[t];
+  const int64_t j = tile_first_run[t] + rank;
+  const int i = valid ? sval[j] : 0;
+  // bank group of the run's start pixel for one load of bpp bytes
+  const int g = bpp < 16 ? bpp : 16;      // bytes a lane loads at once
+  const int ncls = 128 / g, phase = 128 / g;  // bank groups, lanes per phase
+  int cls = ncls;  // empty lanes after every valid one
+  if (valid) {
+    const int lp = run_lp[i];
+    const int ly = lp / ts;
+    const int si = ly * (ts + 1) + (lp - ly * ts);
+    cls = (si * (bpp / g)) % ncls;
+  }
+  int pos = 0;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int c = 0; c <= ncls; ++c) {
+    const unsigned m = __ballot_sync(0xffffffffu, cls == c);
+    if (c < cls) pos += __popc(m);
+    else if (c == cls) pos += __popc(m & lt);
+  }
+  const int phases = 32 / phase;
+  const int nl = phases > 1 ? (pos % phases) * phase + pos / phases : pos;
+  if (!valid) return;
   const unsigned long long k = skey[j];
-  const int t = (int)(k >> rk.tile_shift());
-  const int rank = (int)(j - tile_first_run[t]);
-  const int grp = group_first[t] + rank / 32;
-  const int lane = rank % 32;
   // i: the run's index in emission order (k_runs_emit numbers ray r's runs
   // ray_run_off[r], ray_run_off[r] + 1, ... along the ray), so its ordinal
   // on the ray is i - ray_run_off[r]
-  const int i = sval[j];
-  const int slot = grp * 32 + lane;
+  const int64_t slot = grp * 32 + nl;
   const int64_t r = (int64_t)((k >> 8) & ((1ull << rk.ray_bits) - 1));
   const int ord = (int)(i - ray_run_off[r]);
   gpart[slot] = pbase[r >> 5] + ord * 32 + (int)(r & 31);
   glp[slot] = run_lp[i];
   glen[slot] = run_len[i];
-  run_slot[i] = slot;
+  run_slot[i] = (int)slot;
   atomicMax(&gsteps[grp], (int)run_len[i]);
 }
 
 template <bool L16, int SRC>
 __global__ void __launch_bounds__(kTraceBlock)
-    k_runs_fill(DevGeom G, MatrixDev M, int tiles_x, const int64_t* ray_run_off,
+    k_runs_fill(DevGeom G, MatrixDev M, int tiles_x, int ts, const int64_t* ray_run_off,
                 const int* run_slot, const int64_t* gseg_off,
                 const int64_t* gcode_off, void* tlen, uint32_t* tcode) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -220,7 +260,7 @@ __global__ void __launch_bounds__(kTraceBlock)
     }
   };
   ray_segments<SRC, L16>(G, M, r, [&](int, int ix, int iy, float l, uint16_t code) {
-    const int t = tile_of(G, ix, iy, tiles_x);
+    const int t = tile_of(ix, iy, tiles_x, ts);
     if (t != cur || !unit_step(ix, iy, px, py)) {
       flush();
       ++i;
@@ -232,7 +272,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       lbase = gseg_off[grp] + lane * 8;
       cbase = gcode_off[grp] + lane * 2;
     } else {
-      const uint32_t b = (uint32_t)((ix - px) + (iy - py) * RS) & 0xffu;
+      const uint32_t b = (uint32_t)((ix - px) + (iy - py) * (ts + 1)) & 0xffu;
       if ((s & 7) < 4) w0 |= b << (8 * (s & 3));
       else w1 |= b << (8 * (s & 3));
     }
@@ -250,20 +290,21 @@ __global__ void __launch_bounds__(kTraceBlock)
 
 // ---- forward -------------------------------------------------------------------
 // Shared-memory image of one tile: K floats per pixel as K/4 float4 planes
-// (K >= 4) or one float/float2 plane, row stride RS pixels; with H, K halves
-// per pixel in one plane (one 16-byte read per segment at K = 8).
+// (K >= 4) or one float/float2 plane, row stride ts + 1 pixels; with H, K
+// halves per pixel in one plane (one 16-byte read per segment at K = 8).
 template <int K, bool H = false>
 struct TilePlanes {
   static constexpr int kPlanes = K >= 4 ? K / 4 : 1;
   static constexpr int kWidth = K >= 4 ? 4 : K;  // floats per plane entry
-  static constexpr int kBytes = TS * RS * K * (H ? 2 : 4);
+  static int bytes(int ts) { return ts * (ts + 1) * K * (H ? 2 : 4); }
 };
 
 template <int K>
 __device__ __forceinline__ void tile_load_half(__half* sm, const float* __restrict__ recon,
-                                               int g, int x0, int y0) {
-  for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) {
-    const int lx = e % TS, ly = e / TS;
+                                               int g, int x0, int y0, int ts) {
+  const int rs = ts + 1;
+  for (int e = threadIdx.x; e < ts * ts; e += blockDim.x) {
+    const int ly = e / ts, lx = e - ly * ts;
     const int x = x0 + lx, y = y0 + ly;
     Vec<K> v;
     if (x < g && y < g) {
@@ -272,7 +313,7 @@ __device__ __forceinline__ void tile_load_half(__half* sm, const float* __restri
 #pragma unroll
       for (int j = 0; j < K; ++j) v.v[j] = 0.f;
     }
-    store_hvec<K>(sm + (ly * RS + lx) * K, v);
+    store_hvec<K>(sm + (ly * rs + lx) * K, v);
   }
 }
 
@@ -285,18 +326,19 @@ __device__ __forceinline__ void tile_fma_half(const __half* sm, int si, float l,
 
 template <int K>
 __device__ __forceinline__ void tile_load(float* sm, const float* __restrict__ recon,
-                                          int g, int x0, int y0) {
+                                          int g, int x0, int y0, int ts) {
   constexpr int W = TilePlanes<K>::kWidth;
   constexpr int NP = TilePlanes<K>::kPlanes;
-  for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) {
-    const int lx = e % TS, ly = e / TS;
+  const int rs = ts + 1;
+  for (int e = threadIdx.x; e < ts * ts; e += blockDim.x) {
+    const int ly = e / ts, lx = e - ly * ts;
     const int x = x0 + lx, y = y0 + ly;
-    const int si = ly * RS + lx;
+    const int si = ly * rs + lx;
     const bool in = x < g && y < g;
     const float* src = recon + ((int64_t)y * g + x) * K;
 #pragma unroll
     for (int pl = 0; pl < NP; ++pl) {
-      float* dst = sm + ((size_t)pl * TS * RS + si) * W;
+      float* dst = sm + ((size_t)pl * ts * rs + si) * W;
       if constexpr (W == 4) {
         *reinterpret_cast<float4*>(dst) =
             in ? __ldg(reinterpret_cast<const float4*>(src) + pl)
@@ -311,14 +353,15 @@ __device__ __forceinline__ void tile_load(float* sm, const float* __restrict__ r
   }
 }
 
+// plane: floats of one plane (ts * (ts + 1) pixels x plane width)
 template <int K>
-__device__ __forceinline__ void tile_fma(const float* sm, int si, float l,
+__device__ __forceinline__ void tile_fma(const float* sm, int si, float l, int plane,
                                          float (&acc)[K]) {
   constexpr int W = TilePlanes<K>::kWidth;
   constexpr int NP = TilePlanes<K>::kPlanes;
 #pragma unroll
   for (int pl = 0; pl < NP; ++pl) {
-    const float* src = sm + ((size_t)pl * TS * RS + si) * W;
+    const float* src = sm + (size_t)pl * plane + (size_t)si * W;
     if constexpr (W == 4) {
       const float4 v = *reinterpret_cast<const float4*>(src);
       acc[pl * 4 + 0] = fmaf(v.x, l, acc[pl * 4 + 0]);
@@ -393,21 +436,25 @@ __device__ __forceinline__ float chunk_len(const Chunk<LK>& ch, int j,
 // COMP: compensated summation - each chunk's 8 products are an FMA chain
 // added to the run's sum with Kahan's correction (the stored partial sum is
 // the corrected one).
+// One block's work: tile block / splits of matrix T (see k_forward_tiled).
 template <int K, int LK, bool H, bool COMP>
-__global__ void __launch_bounds__(kBlock)
-    k_forward_tiled(TileMatrixDev T, int g, float inv_scale, int splits,
-                    const float* __restrict__ recon, float* __restrict__ part) {
+__device__ __forceinline__ void forward_tiled_block(const TileMatrixDev& T, int g,
+                                                    float inv_scale, int splits, int block,
+                                                    const float* __restrict__ recon,
+                                                    float* __restrict__ part) {
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   __half* smh = reinterpret_cast<__half*>(smem4);
   // `splits` blocks share a tile (small grids: fewer tiles than SMs); each
   // loads the tile and takes every splits-th warp group
-  const int t = blockIdx.x / splits, sub = blockIdx.x - t * splits;
-  const int x0 = (t % T.tiles_x) * TS, y0 = (t / T.tiles_x) * TS;
+  const int t = block / splits, sub = block - t * splits;
+  const int ts = T.ts, rs = ts + 1;
+  const int x0 = (t % T.tiles_x) * ts, y0 = (t / T.tiles_x) * ts;
+  const int plane = ts * rs * TilePlanes<K>::kWidth;
   if constexpr (H)
-    tile_load_half<K>(smh, recon, g, x0, y0);
+    tile_load_half<K>(smh, recon, g, x0, y0, ts);
   else
-    tile_load<K>(sm, recon, g, x0, y0);
+    tile_load<K>(sm, recon, g, x0, y0, ts);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g0 = T.group_first[t], g1 = T.group_first[t + 1];
@@ -415,7 +462,8 @@ __global__ void __launch_bounds__(kBlock)
     const int slot = grp * 32 + lane;
     const int pslot = T.gpart[slot];
     const int lp = T.glp[slot];
-    int si = (lp / TS) * RS + lp % TS;  // shared-memory index of the current pixel
+    const int ly = lp / ts;
+    int si = ly * rs + (lp - ly * ts);  // shared-memory index of the current pixel
     const int chunks = (T.gsteps[grp] + 7) >> 3;
     const int64_t lb = T.gseg_off[grp] + lane * 8;
     const int64_t cb = T.gcode_off[grp] + lane * 2;
@@ -435,7 +483,7 @@ __global__ void __launch_bounds__(kBlock)
         if constexpr (H)
           tile_fma_half<K>(smh, si, chunk_len<LK>(cur, j, inv_scale), a);
         else
-          tile_fma<K>(sm, si, chunk_len<LK>(cur, j, inv_scale), a);
+          tile_fma<K>(sm, si, chunk_len<LK>(cur, j, inv_scale), plane, a);
       }
     };
     for (int c = 0; c < chunks; ++c) {
@@ -464,18 +512,33 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+template <int K, int LK, bool H, bool COMP>
+__global__ void __launch_bounds__(kBlock)
+    k_forward_tiled(TileMatrixDev T, int g, float inv_scale, int splits,
+                    const float* __restrict__ recon, float* __restrict__ part) {
+  forward_tiled_block<K, LK, H, COMP>(T, g, inv_scale, splits, blockIdx.x, recon, part);
+}
+
+// Many plans' forward projections in one launch: block -> work item (a
+// plan's slice batch) through the items' first blocks, one block per tile.
+template <int K, int LK, bool H, bool COMP>
+__global__ void __launch_bounds__(kBlock)
+    k_forward_tiled_multi(const FwdItem* __restrict__ items, int nitems) {
+  const FwdItem& it = items[item_of(items, nitems, blockIdx.x)];
+  forward_tiled_block<K, LK, H, COMP>(it.T, it.g, it.inv_scale, 1,
+                                      (int)(blockIdx.x - it.first), it.recon, it.part);
+}
+
 // A ray's partial sums (its runs' slots, in path order) -> per-ray factor,
 // as k_forward's epilogue. FH (ratio factors only): the factor is stored as
 // the half (ray/sim - 1).
 template <int K, bool FH, bool COMP>
-__global__ void k_fwd_finish(int64_t nrays, const int* __restrict__ rnrun,
-                             const int* __restrict__ pbase,
-                             const float* __restrict__ ra2,
-                             const float* __restrict__ part,
-                             const float* __restrict__ sino,
-                             float* __restrict__ out, int out_mode) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrays) return;
+__device__ __forceinline__ void fwd_finish_ray(int64_t r, const int* __restrict__ rnrun,
+                                               const int* __restrict__ pbase,
+                                               const float* __restrict__ ra2,
+                                               const float* __restrict__ part,
+                                               const float* __restrict__ sino,
+                                               float* __restrict__ out, int out_mode) {
   Vec<K> s;
   float cmp[K];
 #pragma unroll
@@ -515,10 +578,35 @@ __global__ void k_fwd_finish(int64_t nrays, const int* __restrict__ rnrun,
   }
 }
 
+template <int K, bool FH, bool COMP>
+__global__ void k_fwd_finish(int64_t nrays, const int* __restrict__ rnrun,
+                             const int* __restrict__ pbase,
+                             const float* __restrict__ ra2,
+                             const float* __restrict__ part,
+                             const float* __restrict__ sino,
+                             float* __restrict__ out, int out_mode) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nrays) fwd_finish_ray<K, FH, COMP>(r, rnrun, pbase, ra2, part, sino, out, out_mode);
+}
+
+// Many plans' finishes in one launch: block -> work item, 256 rays a block.
+template <int K, bool COMP>
+__global__ void k_fwd_finish_multi(const FinItem* __restrict__ items, int nitems) {
+  const FinItem& it = items[item_of(items, nitems, blockIdx.x)];
+  const int64_t r = (int64_t)(blockIdx.x - it.first) * blockDim.x + threadIdx.x;
+  if (r >= it.nrays) return;
+  if (it.fh)
+    fwd_finish_ray<K, true, COMP>(r, it.rnrun, it.pbase, it.ra2, it.part, it.sino, it.out,
+                                  it.out_mode);
+  else
+    fwd_finish_ray<K, false, COMP>(r, it.rnrun, it.pbase, it.ra2, it.part, it.sino, it.out,
+                                   it.out_mode);
+}
+
 template <int K, int LK, bool H, bool COMP>
 void fwd_tiled_launch(const TileMatrixDev& T, int g, float inv_scale,
                       const float* recon, float* part, cudaStream_t st) {
-  const int smem = TilePlanes<K, H>::kBytes;
+  const int smem = TilePlanes<K, H>::bytes(T.ts);
   cudaFuncSetAttribute(k_forward_tiled<K, LK, H, COMP>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   // at least two blocks per SM when the grid has few tiles
@@ -552,10 +640,12 @@ void fwd_tiled_half(const IterArgs& A, const TileMatrixDev& T, const float* reco
     fwd_tiled_kind<K, false, COMP>(T, A.G.C, A.M.len_kind, A.M.inv_scale, recon, part, st);
 }
 
+// compensated sums: up to 8 slices per pass (plan creation checks)
 template <int K>
 void fwd_tiled_comp(const IterArgs& A, const TileMatrixDev& T, const float* recon,
                     float* part, cudaStream_t st) {
-  if (A.comp) fwd_tiled_half<K, true>(A, T, recon, part, st);
+  constexpr bool kComp = K <= 8;
+  if (kComp && A.comp) fwd_tiled_half<K, kComp>(A, T, recon, part, st);
   else fwd_tiled_half<K, false>(A, T, recon, part, st);
 }
 
@@ -568,7 +658,7 @@ static int seg_source(const MatrixDev& M) {
   return M.rcode != nullptr ? kSrcDelta : kSrcIndex;
 }
 
-void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, RunKey rk,
+void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts, RunKey rk,
                       const int64_t* ray_run_off, unsigned long long* key, int* val,
                       uint16_t* run_lp, uint16_t* run_len, int* tile_count,
                       cudaStream_t st) {
@@ -577,15 +667,15 @@ void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, RunKey 
   switch (seg_source(M)) {
     case kSrcDelta:
       k_runs_emit<kSrcDelta><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+          G, M, tiles_x, ts, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
       break;
     case kSrcIndex:
       k_runs_emit<kSrcIndex><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+          G, M, tiles_x, ts, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
       break;
     default:
       k_runs_emit<kSrcTrace><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+          G, M, tiles_x, ts, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
   }
 }
 
@@ -606,19 +696,19 @@ int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
 }
 
 void launch_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
-                       int64_t nruns, const int* tile_first_run,
+                       int ntiles, int64_t ngroups, const int* tile_first_run,
                        const int* group_first, const uint16_t* run_lp,
                        const uint16_t* run_len, const int64_t* ray_run_off,
-                       const int* pbase, int* gpart, uint16_t* glp,
-                       uint16_t* glen, int* gsteps, int* run_slot,
-                       cudaStream_t st) {
-  k_runs_group<<<blocks_for(nruns, 256), 256, 0, st>>>(
-      rk, skey, sval, nruns, tile_first_run, group_first, run_lp, run_len, ray_run_off,
-      pbase, gpart, glp, glen, gsteps, run_slot);
+                       const int* pbase, int ts, int bpp, int* gpart, uint16_t* glp,
+                       uint16_t* glen, int* gsteps, int* run_slot, cudaStream_t st) {
+  const int64_t threads = ngroups * 32;
+  k_runs_group<<<blocks_for(threads, 256), 256, 0, st>>>(
+      rk, skey, sval, ntiles, ngroups, tile_first_run, group_first, run_lp, run_len,
+      ray_run_off, pbase, ts, bpp, gpart, glp, glen, gsteps, run_slot);
 }
 
 template <bool L16>
-static void runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x,
+static void runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts,
                       const int64_t* ray_run_off, const int* run_slot,
                       const int64_t* gseg_off, const int64_t* gcode_off, void* tlen,
                       uint32_t* tcode, cudaStream_t st) {
@@ -627,27 +717,27 @@ static void runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x,
   switch (seg_source(M)) {
     case kSrcDelta:
       k_runs_fill<L16, kSrcDelta><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
+          G, M, tiles_x, ts, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
       break;
     case kSrcIndex:
       k_runs_fill<L16, kSrcIndex><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
+          G, M, tiles_x, ts, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
       break;
     default:
       k_runs_fill<L16, kSrcTrace><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
+          G, M, tiles_x, ts, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
   }
 }
 
-void launch_runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x,
+void launch_runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts,
                       const int64_t* ray_run_off, const int* run_slot,
                       const int64_t* gseg_off, const int64_t* gcode_off,
                       void* tlen, uint32_t* tcode, cudaStream_t st) {
   if (M.len_kind != LK_F32)
-    runs_fill<true>(G, M, tiles_x, ray_run_off, run_slot, gseg_off, gcode_off, tlen,
+    runs_fill<true>(G, M, tiles_x, ts, ray_run_off, run_slot, gseg_off, gcode_off, tlen,
                     tcode, st);
   else
-    runs_fill<false>(G, M, tiles_x, ray_run_off, run_slot, gseg_off, gcode_off, tlen,
+    runs_fill<false>(G, M, tiles_x, ts, ray_run_off, run_slot, gseg_off, gcode_off, tlen,
                      tcode, st);
 }
 
@@ -671,8 +761,9 @@ void fwd_finish_k(const IterArgs& A, const TileMatrixDev& T, const float* part,
   k_fwd_finish<K, FH, CP><<<b, 256, 0, st>>>(R, T.rnrun, T.pbase, A.M.ra2, part, sino, \
                                              out, out_mode)
   const bool fh = A.half_factors && out_mode == FWD_RATIO;
-  if (A.comp) {
-    if (fh) TG_FINISH(true, true); else TG_FINISH(false, true);
+  constexpr bool kComp = K <= 8;
+  if (kComp && A.comp) {
+    if (fh) TG_FINISH(true, kComp); else TG_FINISH(false, kComp);
   } else {
     if (fh) TG_FINISH(true, false); else TG_FINISH(false, false);
   }
@@ -687,6 +778,65 @@ void launch_fwd_finish(const IterArgs& A, const TileMatrixDev& T, const float* p
     case 4: fwd_finish_k<4>(A, T, part, sino, out, out_mode, st); break;
     case 8: fwd_finish_k<8>(A, T, part, sino, out, out_mode, st); break;
     default: fwd_finish_k<16>(A, T, part, sino, out, out_mode, st); break;
+  }
+}
+
+template <int K, int LK, bool H, bool COMP>
+static void fwd_multi_launch(const FwdItem* items, int n, int64_t blocks, int ts,
+                             cudaStream_t st) {
+  const int smem = TilePlanes<K, H>::bytes(ts);
+  cudaFuncSetAttribute(k_forward_tiled_multi<K, LK, H, COMP>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  k_forward_tiled_multi<K, LK, H, COMP><<<(unsigned)blocks, kBlock, smem, st>>>(items, n);
+}
+
+// the multi-plan path serves 16-bit fixed-point lengths only
+template <int K, bool H, bool COMP>
+static void fwd_multi_kind(const FwdItem* items, int n, int64_t blocks, int ts,
+                           cudaStream_t st) {
+  fwd_multi_launch<K, LK_U16, H, COMP>(items, n, blocks, ts, st);
+}
+
+template <int K>
+static void fwd_multi_k(const FwdItem* items, int n, int64_t blocks, int ts, int half_tile,
+                        int comp, cudaStream_t st) {
+  constexpr bool kComp = K <= 8;
+  if (K == 16 || half_tile) {
+    if (kComp && comp) fwd_multi_kind<K, true, kComp>(items, n, blocks, ts, st);
+    else fwd_multi_kind<K, true, false>(items, n, blocks, ts, st);
+  } else if constexpr (K != 16) {
+    if (comp) fwd_multi_kind<K, false, true>(items, n, blocks, ts, st);
+    else fwd_multi_kind<K, false, false>(items, n, blocks, ts, st);
+  }
+}
+
+void launch_forward_tiled_multi(const FwdItem* items, int n, int64_t blocks, int K, int ts,
+                                int half_tile, int comp, cudaStream_t st) {
+  switch (K) {
+    case 1: fwd_multi_k<1>(items, n, blocks, ts, half_tile, comp, st); break;
+    case 2: fwd_multi_k<2>(items, n, blocks, ts, half_tile, comp, st); break;
+    case 4: fwd_multi_k<4>(items, n, blocks, ts, half_tile, comp, st); break;
+    case 8: fwd_multi_k<8>(items, n, blocks, ts, half_tile, comp, st); break;
+    default: fwd_multi_k<16>(items, n, blocks, ts, half_tile, comp, st); break;
+  }
+}
+
+template <int K>
+static void finish_multi_k(const FinItem* items, int n, int64_t blocks, int comp,
+                           cudaStream_t st) {
+  constexpr bool kComp = K <= 8;
+  if (kComp && comp) k_fwd_finish_multi<K, kComp><<<(unsigned)blocks, 256, 0, st>>>(items, n);
+  else k_fwd_finish_multi<K, false><<<(unsigned)blocks, 256, 0, st>>>(items, n);
+}
+
+void launch_fwd_finish_multi(const FinItem* items, int n, int64_t blocks, int K, int comp,
+                             cudaStream_t st) {
+  switch (K) {
+    case 1: finish_multi_k<1>(items, n, blocks, comp, st); break;
+    case 2: finish_multi_k<2>(items, n, blocks, comp, st); break;
+    case 4: finish_multi_k<4>(items, n, blocks, comp, st); break;
+    case 8: finish_multi_k<8>(items, n, blocks, comp, st); break;
+    default: finish_multi_k<16>(items, n, blocks, comp, st); break;
   }
 }
 

@@ -17,7 +17,7 @@ constexpr int kTraceBlock = 128;
 
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_count(DevGeom G, int ngroups, int* nseg, int* rcap,
-                  unsigned* maxlen_bits, int tiles_x, int* ray_nruns) {
+                  unsigned* maxlen_bits, int tiles_x, int ts, int* ray_nruns) {
   const int grp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (grp >= ngroups) return;  // warp-uniform
@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       int runs = 0, cur = -1, px = 0, py = 0;
       n = trace_ray(G, a, c, [&](int, float l, float, int ix, int iy) {
         ml = fmaxf(ml, l);
-        const int t = tile_of_pixel(ix, iy, tiles_x);
+        const int t = tile_of_pixel(ix, iy, tiles_x, ts);
         if (t != cur || !unit_step(ix, iy, px, py)) {
           ++runs;
           cur = t;
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       // an exception entry (overflow[2] counts them; past the capacity the
       // plan is refused)
       int tile, tl;
-      pixel_tile(ix, iy, M.tiles_x, &tile, &tl);
+      pixel_tile(ix, iy, M.tiles_x, M.tw_shift, &tile, &tl);
       const unsigned long long k = atomicAdd(overflow + 2, 1ull);
       if (k < (unsigned long long)exc_cap) {
         exc[k] = make_int4(tl, a, c, __float_as_int(l));
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       // backprojection still visits it (0 * a non-finite factor is NaN in
       // the reference too). The 16-bit fixed-point code has no -0.
       int tile, tl;
-      pixel_tile(ix, iy, M.tiles_x, &tile, &tl);
+      pixel_tile(ix, iy, M.tiles_x, M.tw_shift, &tile, &tl);
       const int64_t pos = dense_pair(M.ntiles, a, tile, tl) * 2 + slot;
       if (L16) {
         uint16_t* d = reinterpret_cast<uint16_t*>(dlen);
@@ -157,8 +157,8 @@ __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W, float* Wh
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)M.ntiles * 32) return;
   const int tile = (int)(t >> 5), lane = (int)(t & 31);
-  const int x = (tile % M.tiles_x) * 8 + (lane & 7);
-  const int y = (tile / M.tiles_x) * 4 + (lane >> 3);
+  int x, y;
+  tile_pixel(tile, lane, M.tiles_x, M.tw_shift, &x, &y);
   if (x >= g || y >= g) return;
   const int64_t p = (int64_t)y * g + x;
   float sum = 0.f, comp = 0.f, sumh = 0.f, comph = 0.f;
@@ -222,12 +222,12 @@ __global__ void __launch_bounds__(kTraceBlock)
 }  // namespace
 
 void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
-                        unsigned* maxlen_bits, int tiles_x, int* ray_nruns,
+                        unsigned* maxlen_bits, int tiles_x, int ts, int* ray_nruns,
                         cudaStream_t st) {
   const int ngroups = G.P * G.gpa;
   const int blocks = (ngroups * 32 + kTraceBlock - 1) / kTraceBlock;
   k_trace_count<<<blocks, kTraceBlock, 0, st>>>(G, ngroups, nseg, rcap,
-                                                 maxlen_bits, tiles_x, ray_nruns);
+                                                 maxlen_bits, tiles_x, ts, ray_nruns);
 }
 
 void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,

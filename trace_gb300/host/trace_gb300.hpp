@@ -48,6 +48,8 @@ struct Options {
   int half_gathers = 0;     // fast mode + forward_tiles: 16-bit gather operands
   int forward_on_the_fly = 0;  // trace rays during the forward projection
   int compensated = 0;      // fast mode + forward_tiles: Kahan ray/pixel sums
+  int backward_tile_width = 0;  // 8 (default), 16 or 4 pixels per tile row
+  int forward_tile_side = 0;    // 64 (default), 32 or 96
 };
 
 // Geometry + reconstruction (TraceMetadata). theta is copied, not owned.
@@ -84,6 +86,8 @@ class GpuTraceMetadata {
     d.half_gathers = opt.half_gathers;
     d.forward_on_the_fly = opt.forward_on_the_fly;
     d.compensated = opt.compensated;
+    d.backward_tile_width = opt.backward_tile_width;
+    d.forward_tile_side = opt.forward_tile_side;
     tg_plan* p = nullptr;
     check(tg_plan_create(&d, theta, nullptr, nullptr, &p), nullptr);
     plan_.reset(p);
