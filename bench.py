@@ -75,7 +75,14 @@ WORKLOADS = {
                          "MLEM, 1024x1024 grid, 64 slices, 720 angles x 1024 columns, "
                          "20 iterations, Poisson noise I0=5e3, sinogram clipped at 1e-6")),
     "apmlr2048": dict(alg="apmlr", C=2048, P=1500, S=2048, iters=25, beta=0.02, i0=2e4,
-                      volume=True, plain_slices=8, fp64_slices=8, name=(
+                      volume=True, plain_slices=8, fp64_slices=8,
+                      # the workload description asks for "acceleration on"; the
+                      # reference's APMLR has no acceleration option
+                      # (src/apmlr/apmlr_main.cc:20-26), so there is nothing to
+                      # match and nothing is implemented under that name
+                      acceleration=("not implemented: the reference's APMLR has no "
+                                    "acceleration option (src/apmlr/apmlr_main.cc:20-26)"),
+                      name=(
                           "APMLR 8-neighbour regulariser beta0=0.02 (beta1, delta0, "
                           "delta1, regw 1), full volume 2048 slices x 2048x2048 grid, "
                           "1500 angles x 2048 columns, 25 iterations, random-ellipsoid "
@@ -452,7 +459,8 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
                    mode="fast", delta_index=True, forward_tiles=args.tiles,
                    backward_staged=args.staged, half_gathers=args.half,
                    forward_on_the_fly=args.otf, compensated=args.compensated,
-                   forward_tile_side=args.fts, backward_tile_width=args.btw)
+                   forward_tile_side=args.fts, backward_tile_width=args.btw,
+                   batch_streams=args.batch_streams)
     plan.set_stream(stream)
     info = plan.info()
     sino = make_data(W, dev, plan)
@@ -569,6 +577,8 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
                    "backward_tile": {4: "4x8", 16: "16x2"}.get(args.btw, "8x4") + " pixels",
                    "step": f"one {alg.upper()} iteration over all {S} slices",
                    "graphs": bool(args.graphs),
+                   "batch_streams": args.batch_streams,
+                   **({"acceleration": W["acceleration"]} if W.get("acceleration") else {}),
                    "summation": "compensated (Kahan over 8-segment / 4-angle blocks)"
                                 if args.compensated else "FMA chains",
                    "l2": "inputs larger than L2 (system matrix "
@@ -1043,6 +1053,9 @@ def main():
                     help="backprojection tile width (4, 8, 16; 0 = the plan default)")
     ap.add_argument("--compensated", action="store_true",
                     help="compensated (Kahan) ray and pixel sums in the measured path")
+    ap.add_argument("--batch-streams", type=int, default=0,
+                    help="1: every slice batch on one stream; 2 (0 = default): odd "
+                         "batches on a second stream")
     ap.add_argument("--no-graphs", dest="graphs", action="store_false",
                     help="eager launches instead of one CUDA graph per iteration")
     ap.add_argument("--no-plain", dest="plain", action="store_false")

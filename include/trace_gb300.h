@@ -36,8 +36,11 @@
  * message of the last failure on a plan is tg_last_error(plan) (or
  * tg_last_error(NULL) for a failed tg_plan_create). No call throws. The
  * library owns device memory; callers own host buffers. Each plan issues its
- * work on one CUDA stream (its own, or one given with tg_plan_set_stream).
- * Calls on one plan are not thread-safe; distinct plans are independent.
+ * work on one CUDA stream (its own, or one given with tg_plan_set_stream);
+ * tg_iterate may fork part of an iteration onto the plan's own second stream
+ * (batch_streams) and joins it back into that stream before returning, so
+ * callers see stream order as if one stream did all the work. Calls on one
+ * plan are not thread-safe; distinct plans are independent.
  */
 #ifndef TRACE_GB300_H
 #define TRACE_GB300_H
@@ -97,9 +100,10 @@ typedef struct {
                              projection of slice s reads reconstruction slice
                              s-1 (apmlr.cc:1083-1084); 1 = reads slice s */
   int forward_tiles;      /* fast mode only: tg_iterate runs the forward
-                             projection through 64x64 reconstruction tiles
-                             staged in shared memory (an extra tile-ordered
-                             copy of the forward matrix is built) */
+                             projection through square reconstruction tiles
+                             (forward_tile_side) staged in shared memory (an
+                             extra tile-ordered copy of the forward matrix
+                             is built) */
   int backward_staged;    /* fast mode only: the backprojection stages each
                              16x16-pixel block's detector windows in shared
                              memory instead of gathering through L1 */
@@ -141,6 +145,14 @@ typedef struct {
                               96; the tile of slices_per_pass slices must fit
                               shared memory (96 needs half_gathers and at
                               most 8 slices per pass) */
+  int batch_streams;       /* forward_tiles with two or more slice batches:
+                              2 (0 selects it) - tg_iterate runs odd batches
+                              on a second stream with their own partial sums
+                              and factors (one more partial-sum buffer), so
+                              one batch's forward projection overlaps the
+                              previous batch's finish and backprojection;
+                              1 - every batch on the plan's stream. Results
+                              are the same bits either way */
 } tg_plan_desc;
 
 typedef struct {

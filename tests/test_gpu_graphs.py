@@ -137,3 +137,27 @@ def test_batch_with_an_ineligible_plan_uses_per_plan_graph():
     batch.close()
     for p in plans:
         p.close()
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+@pytest.mark.parametrize("alg", ["sirt", "mlem", "pml", "apmlr"])
+def test_two_stream_iterations_match_one_stream(graphs, alg):
+    """batch_streams = 2 (odd slice batches on the plan's second stream, with
+    their own partial sums and factors) gives the same bits as one stream,
+    eagerly and replayed from CUDA graphs; a user stream set on the plan
+    still sees the whole iteration in its order."""
+    import torch
+    prm = tg.default_params(alg, beta=0.3)
+    outs = []
+    for streams in (1, 2):
+        plan = _plan(96, 70, 21, 3, alg, slices_per_pass=4, mode="fast", len_storage="u16",
+                     delta_index=True, forward_tiles=True, half_gathers=True,
+                     batch_streams=streams)
+        user = torch.cuda.Stream()
+        plan.set_stream(user.cuda_stream)
+        plan.set_graphs(graphs)
+        plan.iterate(alg, 3, prm)
+        plan.iterate(alg, 2, prm)
+        outs.append(plan.get_recon(alg))
+        plan.close()
+    assert np.array_equal(bits(outs[0]), bits(outs[1]))

@@ -44,6 +44,14 @@ struct tg_plan {
   bool tiles = false;
   TileMatrixDev T{};
   float* d_part = nullptr;
+  // two-stream iterations (batch_streams): odd slice batches run on st2
+  // with their own partial sums and factors, so one batch's forward
+  // projection overlaps the previous batch's finish and backprojection
+  bool two = false;
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  float* d_part2 = nullptr;
+  float* d_upd2 = nullptr;
   // FP64 mode: double state, factors, total lengths and SIRT's a2
   bool fp64 = false;
   double *d_ra2d = nullptr, *d_W64 = nullptr;
@@ -457,8 +465,9 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
 }
 
 int ensure_upd(tg_plan* p) {
-  if (p->d_upd) return TG_OK;
-  return dalloc(p, &p->d_upd, (size_t)p->R * p->K * (p->fp64 ? 2 : 1));
+  if (!p->d_upd) TG_TRY(dalloc(p, &p->d_upd, (size_t)p->R * p->K * (p->fp64 ? 2 : 1)));
+  if (p->two && !p->d_upd2) TG_TRY(dalloc(p, &p->d_upd2, (size_t)p->R * p->K));
+  return TG_OK;
 }
 
 int fp32_only(tg_plan* p) {
@@ -540,6 +549,8 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
                       " bytes) does not fit shared memory; use a smaller "
                       "forward_tile_side, fewer slices per pass or half_gathers");
   }
+  if (d.batch_streams < 0 || d.batch_streams > 2)
+    return fail(nullptr, TG_E_ARG, "batch_streams must be 0, 1 or 2");
   if (d.backward_tile_width != 0 && d.backward_tile_width != 4 &&
       d.backward_tile_width != 8 && d.backward_tile_width != 16)
     return fail(nullptr, TG_E_ARG, "backward_tile_width must be 0, 4, 8 or 16");
@@ -828,6 +839,18 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     if (p->err.empty()) p->err = "building the tile-ordered forward matrix failed";
     return bail(rc);
   }
+  // two-stream iterations: tile-staged plans with two or more slice batches
+  if (p->tiles && p->nb >= 2 && d.batch_streams != 1) {
+    if (cudaStreamCreateWithFlags(&p->st2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      p->err = "creating the second stream failed";
+      return bail(TG_E_CUDA);
+    }
+    if ((rc = dalloc(p, &p->d_part2, (size_t)p->info.partial_slots * p->K))) return bail(rc);
+    p->two = true;
+  }
   cudaEventRecord(e1, p->st);
   cudaEventSynchronize(e1);
   float ms = 0.f;
@@ -902,6 +925,10 @@ int tg_plan_destroy(tg_plan* p) {
   for (auto ev : p->ev_pool) cudaEventDestroy(ev);
   for (void* a : p->allocs)
     if (a) cudaFree(a);
+  if (p->st2) cudaStreamSynchronize(p->st2);
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  if (p->ev_join) cudaEventDestroy(p->ev_join);
+  if (p->st2) cudaStreamDestroy(p->st2);
   if (p->own) cudaStreamDestroy(p->own);
   delete p;
   return TG_OK;
@@ -1058,32 +1085,46 @@ static int half_factors_next(const tg_plan* p, int mode) {
 
 // Launches of one fused iteration on the plan's stream (buffers by p->cur;
 // the caller flips p->cur and counts the iteration).
-static void issue_iteration(tg_plan* p, const IterArgs& A0, int mode) {
+// two_streams: the plan's odd slice batches go to its second stream (forked
+// from and joined back into p->st), except while the per-kernel timers run.
+static void issue_iteration(tg_plan* p, const IterArgs& A0, int mode, bool two_streams) {
   IterArgs A = A0;
   if (p->tiles && p->d.half_gathers) {
     A.half_tile = 1;
     A.half_factors = half_factors_next(p, mode);
   }
+  const bool two = two_streams && p->two && !p->timing;
+  if (two) {
+    cudaEventRecord(p->ev_fork, p->st);
+    cudaStreamWaitEvent(p->st2, p->ev_fork, 0);
+  }
   for (int b = 0; b < p->nb; ++b) {
+    const bool odd = two && (b & 1);
+    const cudaStream_t s = odd ? p->st2 : p->st;
+    float* upd = odd ? p->d_upd2 : p->d_upd;
     if (p->tiles) {
+      float* part = odd ? p->d_part2 : p->d_part;
       const float* src = batch_ptr(p, p->d_recon[p->cur], b * p->K + p->fshift);
       {
         Timed t(p, 0);
-        launch_forward_tiled(A, p->T, src, p->d_part, p->st);
+        launch_forward_tiled(A, p->T, src, part, s);
       }
       Timed t(p, 2);
-      launch_fwd_finish(A, p->T, p->d_part, p->d_sino + (int64_t)b * p->R * p->K,
-                        p->d_upd, mode, p->st);
+      launch_fwd_finish(A, p->T, part, p->d_sino + (int64_t)b * p->R * p->K, upd, mode, s);
     } else {
-      run_forward(p, A, b, mode, p->d_upd);
+      run_forward(p, A, b, mode, upd);
     }
     Timed t(p, 1);
     if (!p->d.backward_staged)
-      launch_backward(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
-                      p->d_upd, nullptr, EPI_UPDATE, p->st);
+      launch_backward(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1], upd, nullptr,
+                      EPI_UPDATE, s);
     else
-      launch_backward_staged(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1],
-                             p->d_upd, nullptr, EPI_UPDATE, p->st);
+      launch_backward_staged(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1], upd,
+                             nullptr, EPI_UPDATE, s);
+  }
+  if (two) {
+    cudaEventRecord(p->ev_join, p->st2);
+    cudaStreamWaitEvent(p->st, p->ev_join, 0);
   }
 }
 
@@ -1143,7 +1184,7 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
         g = tg_plan::Graph();
         cudaGraph_t graph;
         TG_CUDA(p, cudaStreamBeginCapture(p->st, cudaStreamCaptureModeThreadLocal));
-        issue_iteration(p, A, mode);
+        issue_iteration(p, A, mode, true);
         TG_CUDA(p, cudaStreamEndCapture(p->st, &graph));
         const cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
         cudaGraphDestroy(graph);
@@ -1155,7 +1196,7 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
       }
       TG_CUDA(p, cudaGraphLaunch(g.exec, p->st));
     } else {
-      issue_iteration(p, A, mode);
+      issue_iteration(p, A, mode, true);
     }
     p->cur ^= 1;
     ++p->iters_done;
@@ -1548,7 +1589,7 @@ extern "C" int tg_batch_iterate(tg_batch* b, const int* algs, const tg_params* p
         const cudaStream_t keep = p->st;
         p->st = b->streams[i % ns];
         const IterArgs A = make_args(p, algs[i], params ? &params[i] : nullptr);
-        issue_iteration(p, A, algs[i] == TG_SIRT ? FWD_SIRT : FWD_RATIO);
+        issue_iteration(p, A, algs[i] == TG_SIRT ? FWD_SIRT : FWD_RATIO, false);
         p->st = keep;
       }
       for (int s = 0; e == cudaSuccess && s < ns; ++s) {
