@@ -78,7 +78,7 @@ struct TileMatrixDev {
                             // run, -1 if the lane is empty
   const int* rnrun;         // [P*C] runs of each ray
   const int* pbase;         // [ceil(P*C / 32)] first slot of each ray group
-  const uint16_t* glp;      // [groups * 32] first pixel, tile-local (y*64 + x)
+  const uint16_t* glp;      // [groups * 32] first pixel, tile-local (y*ts + x)
   const uint16_t* glen;     // [groups * 32] run length (segments)
   const int* gsteps;        // [groups] longest run of the group
   const int64_t* gseg_off;  // [groups] entry offset of the group's lengths
@@ -265,13 +265,11 @@ void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts,
 int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
               int* val_in, int* val_out, int64_t n, int end_bit,
               cudaStream_t st);
-// lanes of each 32-run group, dealt by the bank group of the runs' start
-// pixels in the shared-memory tile (bpp: bytes per pixel of one load)
 void launch_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
-                       int ntiles, int64_t ngroups, const int* tile_first_run,
+                       int64_t nruns, const int* tile_first_run,
                        const int* group_first, const uint16_t* run_lp,
                        const uint16_t* run_len, const int64_t* ray_run_off,
-                       const int* pbase, int ts, int bpp, int* gpart, uint16_t* glp,
+                       const int* pbase, int* gpart, uint16_t* glp,
                        uint16_t* glen, int* gsteps, int* run_slot, cudaStream_t st);
 void launch_runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts,
                       const int64_t* ray_run_off, const int* run_slot,

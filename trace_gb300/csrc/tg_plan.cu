@@ -400,13 +400,8 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
   cudaMemcpyAsync(d_group_first, group_first.data(), (ntiles + 1) * 4, cudaMemcpyHostToDevice, p->st);
   cudaMemcpyAsync(rnrun, nruns.data(), p->R * 4, cudaMemcpyHostToDevice, p->st);
   cudaMemcpyAsync(pbase, pbase_h.data(), rgroups * 4, cudaMemcpyHostToDevice, p->st);
-  // bytes per pixel of one shared-memory load in the forward: K halves (half
-  // tile), or a plane of up to 4 floats
-  const bool half_tile = p->d.half_gathers || p->K == 16;
-  const int bpp = half_tile ? 2 * p->K : 4 * std::min(p->K, 4);
-  launch_runs_group(rk, key2, val2, ntiles, groups, d_tile_first, d_group_first, run_lp,
-                    run_len, d_run_off, pbase, p->fts, bpp, gpart, glp, glen, gsteps,
-                    run_slot, p->st);
+  launch_runs_group(rk, key2, val2, NR, d_tile_first, d_group_first, run_lp, run_len,
+                    d_run_off, pbase, gpart, glp, glen, gsteps, run_slot, p->st);
   std::vector<int> steps(groups);
   cudaMemcpyAsync(steps.data(), gsteps, (size_t)groups * 4, cudaMemcpyDeviceToHost, p->st);
   if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run grouping failed");

@@ -3,7 +3,8 @@
 // The ray-major forward kernel gathers each segment's K reconstruction values
 // through L1/L2: ~1 sector lookup per segment, and at 2048^2 with 8 slices
 // the 134 MB batch no longer stays in L2 next to the streamed matrix. Here
-// the image is cut into 64 x 64 tiles and each ray's segment list into runs
+// the image is cut into ts x ts tiles (ts = 64 by default; 32 or 96 by plan
+// option) and each ray's segment list into runs
 // (consecutive segments inside one tile). One block per tile loads the
 // tile's K-slice reconstruction into shared memory once and walks all runs
 // through it: lane = run, 32 runs of adjacent rays per warp. A lane's
@@ -148,63 +149,25 @@ __global__ void __launch_bounds__(kTraceBlock)
   close();
 }
 
-// One warp per group: the group's 32 runs (consecutive in the sorted order
-// of their tile) get their lanes. The forward reads one pixel per lane and
-// step from the shared-memory tile; lanes of one load phase (8 lanes for a
-// 16-byte load) collide when their pixels fall in the same 16-byte bank
-// group. The runs of a group are adjacent parallel rays that step through
-// the tile nearly in lockstep, their entry points up to sqrt(2) pixels apart
-// along an edge, so consecutive runs can wrap onto the same bank group.
-// Lanes are therefore dealt by the bank group of each run's start pixel:
-// runs sorted by (bank group, rank) go round-robin over the load phases.
-// bpp: bytes per pixel of one shared-memory load (16 for 8 halves or a
-// 4-float plane, 32 for 16 halves, 8 / 4 for fewer slices).
+// One thread per run, in the sorted order of its tile: rank r in the tile is
+// lane r % 32 of the tile's group r / 32.
 __global__ void k_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
-                             int ntiles, int64_t ngroups, const int* tile_first_run,
+                             int64_t nruns, const int* tile_first_run,
                              const int* group_first, const uint16_t* run_lp,
                              const uint16_t* run_len, const int64_t* ray_run_off,
-                             const int* pbase, int ts, int bpp, int* gpart, uint16_t* glp,
+                             const int* pbase, int* gpart, uint16_t* glp,
                              uint16_t* glen, int* gsteps, int* run_slot) {
-  const int64_t grp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (grp >= ngroups) return;  // whole warps
-  // the group's tile: the last t with group_first[t] <= grp
-  int lo = 0, hi = ntiles - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (group_first[mid] <= grp) lo = mid;
-    else hi = mid - 1;
-  }
-  const int t = lo;
-  const int rank = (int)(grp - group_first[t]) * 32 + lane;
-  const bool valid = rank < tile_first_run[t + 1] - tile_first_run[t];
-  const int64_t j = tile_first_run[t] + rank;
-  const int i = valid ? sval[j] : 0;
-  // bank group of the run's start pixel for one load of bpp bytes
-  const int g = bpp < 16 ? bpp : 16;      // bytes a lane loads at once
-  const int ncls = 128 / g, phase = 128 / g;  // bank groups, lanes per phase
-  int cls = ncls;  // empty lanes after every valid one
-  if (valid) {
-    const int lp = run_lp[i];
-    const int ly = lp / ts;
-    const int si = ly * (ts + 1) + (lp - ly * ts);
-    cls = (si * (bpp / g)) % ncls;
-  }
-  int pos = 0;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int c = 0; c <= ncls; ++c) {
-    const unsigned m = __ballot_sync(0xffffffffu, cls == c);
-    if (c < cls) pos += __popc(m);
-    else if (c == cls) pos += __popc(m & lt);
-  }
-  const int phases = 32 / phase;
-  const int nl = phases > 1 ? (pos % phases) * phase + pos / phases : pos;
-  if (!valid) return;
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nruns) return;
   const unsigned long long k = skey[j];
+  const int t = (int)(k >> rk.tile_shift());
+  const int rank = (int)(j - tile_first_run[t]);
+  const int grp = group_first[t] + rank / 32;
   // i: the run's index in emission order (k_runs_emit numbers ray r's runs
   // ray_run_off[r], ray_run_off[r] + 1, ... along the ray), so its ordinal
   // on the ray is i - ray_run_off[r]
-  const int64_t slot = grp * 32 + nl;
+  const int i = sval[j];
+  const int64_t slot = (int64_t)grp * 32 + rank % 32;
   const int64_t r = (int64_t)((k >> 8) & ((1ull << rk.ray_bits) - 1));
   const int ord = (int)(i - ray_run_off[r]);
   gpart[slot] = pbase[r >> 5] + ord * 32 + (int)(r & 31);
@@ -696,15 +659,14 @@ int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
 }
 
 void launch_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
-                       int ntiles, int64_t ngroups, const int* tile_first_run,
+                       int64_t nruns, const int* tile_first_run,
                        const int* group_first, const uint16_t* run_lp,
                        const uint16_t* run_len, const int64_t* ray_run_off,
-                       const int* pbase, int ts, int bpp, int* gpart, uint16_t* glp,
+                       const int* pbase, int* gpart, uint16_t* glp,
                        uint16_t* glen, int* gsteps, int* run_slot, cudaStream_t st) {
-  const int64_t threads = ngroups * 32;
-  k_runs_group<<<blocks_for(threads, 256), 256, 0, st>>>(
-      rk, skey, sval, ntiles, ngroups, tile_first_run, group_first, run_lp, run_len,
-      ray_run_off, pbase, ts, bpp, gpart, glp, glen, gsteps, run_slot);
+  k_runs_group<<<blocks_for(nruns, 256), 256, 0, st>>>(
+      rk, skey, sval, nruns, tile_first_run, group_first, run_lp, run_len, ray_run_off,
+      pbase, gpart, glp, glen, gsteps, run_slot);
 }
 
 template <bool L16>
