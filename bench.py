@@ -446,6 +446,7 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
         args.otf = best.get("forward_on_the_fly", False)
         args.fts = best.get("forward_tile_side", 0)
         args.btw = best.get("backward_tile_width", 0)
+        args.fbw = best.get("forward_block_warps", 0)
         args.slices_per_pass = K
         tuned = {"chosen": best, "sample_slices": n,
                  "ms_per_slice_iter": [[c, round(ms, 4)] for c, ms, _, _ in res]}
@@ -460,7 +461,7 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
                    backward_staged=args.staged, half_gathers=args.half,
                    forward_on_the_fly=args.otf, compensated=args.compensated,
                    forward_tile_side=args.fts, backward_tile_width=args.btw,
-                   batch_streams=args.batch_streams)
+                   batch_streams=args.batch_streams, forward_block_warps=args.fbw)
     plan.set_stream(stream)
     info = plan.info()
     sino = make_data(W, dev, plan)
@@ -575,6 +576,7 @@ def _run_ours(args, W, ws, rank, local, dev, stream, tg, torch, np):
                    "forward": (f"tile-staged ({args.fts or 64}x{args.fts or 64} "
                                "shared-memory tiles)") if args.tiles else "ray-ordered",
                    "backward_tile": {4: "4x8", 16: "16x2"}.get(args.btw, "8x4") + " pixels",
+                   "forward_block_warps": args.fbw or 32,
                    "step": f"one {alg.upper()} iteration over all {S} slices",
                    "graphs": bool(args.graphs),
                    "batch_streams": args.batch_streams,
@@ -632,7 +634,7 @@ def fp64_check(args, W, theta, sino, prm, tg, torch, dev):
                       forward_tiles=args.tiles, backward_staged=args.staged,
                       half_gathers=args.half, slices_per_pass=args.slices_per_pass,
                       compensated=args.compensated, forward_tile_side=args.fts,
-                      backward_tile_width=args.btw),
+                      backward_tile_width=args.btw, forward_block_warps=args.fbw),
         "fp32_same_schedule": dict(len_storage="f32", mode="fast", delta_index=True,
                                    forward_tiles=args.tiles, backward_staged=args.staged,
                                    slices_per_pass=args.slices_per_pass,
@@ -736,7 +738,8 @@ def end_to_end(args, W, theta, sino, prm, tg, torch, stream):
                     delta_index=True, forward_tiles=args.tiles,
                     backward_staged=args.staged, half_gathers=args.half,
                     forward_on_the_fly=args.otf, compensated=args.compensated,
-                    forward_tile_side=args.fts, backward_tile_width=args.btw)
+                    forward_tile_side=args.fts, backward_tile_width=args.btw,
+                    batch_streams=args.batch_streams, forward_block_warps=args.fbw)
         p.set_stream(stream)
         p.set_graphs(args.graphs)
         upload(p, W, host)
@@ -1049,6 +1052,8 @@ def main():
                          "(run the defaults or the flags given)")
     ap.add_argument("--forward-tile-side", dest="fts", type=int, default=0,
                     help="forward tile side (32, 64, 96; 0 = the plan default)")
+    ap.add_argument("--forward-block-warps", dest="fbw", type=int, default=0,
+                    help="warps per forward tile block (8, 16, 32; 0 = the plan default)")
     ap.add_argument("--backward-tile-width", dest="btw", type=int, default=0,
                     help="backprojection tile width (4, 8, 16; 0 = the plan default)")
     ap.add_argument("--compensated", action="store_true",

@@ -153,6 +153,9 @@ typedef struct {
                               previous batch's finish and backprojection;
                               1 - every batch on the plan's stream. Results
                               are the same bits either way */
+  int forward_block_warps; /* forward_tiles: warps of each tile's block, i.e.
+                              runs (one per lane) in flight per tile: 32 (0
+                              selects it), 16 or 8; same results */
 } tg_plan_desc;
 
 typedef struct {

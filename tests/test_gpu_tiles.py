@@ -314,3 +314,26 @@ def test_forward_tile_that_does_not_fit_is_rejected():
         tg.Plan(8, 1, 100, theta_uniform(8), mode="fast", forward_tiles=True,
                 forward_tile_side=48)
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("warps", [8, 16])
+def test_forward_block_warps_are_bit_identical(warps):
+    """Fewer warps per forward tile block (runs in flight per tile) change
+    only the schedule: every run is still one lane's FMA chain into its own
+    slot, so the results are the same bits."""
+    C, P, S = 150, 100, 8
+    th = theta_uniform(P)
+    rng = np.random.default_rng(43)
+    sino = rng.uniform(0.5, 2.0, (P, S, C)).astype(np.float32)
+    prm = tg.default_params("pml", beta=0.1)
+    outs = []
+    for w in (0, warps):
+        plan = tg.Plan(P, S, C, th, slices_per_pass=8, mode="fast", len_storage="u16",
+                       delta_index=True, forward_tiles=True, half_gathers=True,
+                       forward_block_warps=w)
+        plan.set_sinogram(sino, apply_abs=True)
+        plan.reset_recon("pml")
+        plan.iterate("pml", 3, prm)
+        outs.append(plan.get_recon("pml"))
+        plan.close()
+    assert np.array_equal(bits(outs[1]), bits(outs[0]))

@@ -57,7 +57,7 @@ class PlanDesc(C.Structure):
                 ("backward_staged", C.c_int), ("half_gathers", C.c_int),
                 ("forward_on_the_fly", C.c_int), ("compensated", C.c_int),
                 ("backward_tile_width", C.c_int), ("forward_tile_side", C.c_int),
-                ("batch_streams", C.c_int)]
+                ("batch_streams", C.c_int), ("forward_block_warps", C.c_int)]
 
 
 class Params(C.Structure):
@@ -136,7 +136,7 @@ class Plan:
                  num_total_slices=None, sin_tab=None, cos_tab=None,
                  forward_tiles=False, backward_staged=False, half_gathers=False,
                  forward_on_the_fly=False, compensated=False, backward_tile_width=0,
-                 forward_tile_side=0, batch_streams=0):
+                 forward_tile_side=0, batch_streams=0, forward_block_warps=0):
         self._lib = load_library()
         self.P, self.S, self.C = int(num_projs), int(num_slices), int(num_cols)
         d = PlanDesc(self.P, self.S, self.C, float(center), int(slice_id),
@@ -148,7 +148,8 @@ class Plan:
                      int(bool(forward_tiles)), int(bool(backward_staged)),
                      int(bool(half_gathers)), int(bool(forward_on_the_fly)),
                      int(bool(compensated)), int(backward_tile_width),
-                     int(forward_tile_side), int(batch_streams))
+                     int(forward_tile_side), int(batch_streams),
+                     int(forward_block_warps))
         theta = np.ascontiguousarray(theta, np.float32)
         if theta.size != self.P:
             raise ValueError("theta must have num_projs entries")

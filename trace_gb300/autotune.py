@@ -3,7 +3,8 @@
 The choices are those that change how the system matrix is held and
 streamed, not what is computed: slices per pass (K), the forward
 projection's scheduling (ray-ordered gathers vs. shared-memory
-reconstruction tiles, and the tiles' side), the backprojection's (L1 gathers
+reconstruction tiles, the tiles' side and the warps - runs in flight - of
+each tile's block), the backprojection's (L1 gathers
 vs. shared-memory detector windows, and the pixel-tile shape a warp covers),
 and cached vs. on-the-fly ray intersections for the ray-ordered forward
 projection. Each candidate plan is built on a sample of the slices and timed
@@ -36,9 +37,10 @@ DEFAULT_SPACE = {
 REFINE_SPACE = {
     "forward_tile_side": (32, 64, 96),     # forward_tiles: shared-memory tile side
     "backward_tile_width": (4, 8, 16),     # backprojection tiles 4x8, 8x4, 16x2
+    "forward_block_warps": (8, 16, 32),    # forward_tiles: runs in flight per tile
 }
 # what a plan uses when the key is not given
-PLAN_DEFAULTS = {"forward_tile_side": 64, "backward_tile_width": 8}
+PLAN_DEFAULTS = {"forward_tile_side": 64, "backward_tile_width": 8, "forward_block_warps": 32}
 
 TG_E_ARG = 1
 TG_E_NOMEM = 3
@@ -120,7 +122,8 @@ def autotune(theta, sino, alg="pml", params=None, *, len_storage="u16",
     best_cfg, best_ms = min(fitting, key=lambda r: r[1])[:2]
     best_cfg = dict(best_cfg)
     for key, values in refine.items():
-        if key == "forward_tile_side" and not best_cfg.get("forward_tiles"):
+        if key in ("forward_tile_side", "forward_block_warps") and not best_cfg.get(
+                "forward_tiles"):
             continue
         for v in values:
             if key not in best_cfg and v == PLAN_DEFAULTS.get(key):

@@ -73,6 +73,7 @@ __device__ __forceinline__ bool unit_step(int ix, int iy, int px, int py) {
 struct TileMatrixDev {
   int tiles_x, ntiles;
   int ts;                   // tile side (pixels); shared-memory row stride ts + 1
+  int bw;                   // warps per tile block (8, 16 or 32)
   const int* group_first;   // [ntiles + 1] first group of each tile
   const int* gpart;         // [groups * 32] partial-sum slot of each lane's
                             // run, -1 if the lane is empty
@@ -286,7 +287,7 @@ void launch_fwd_finish(const IterArgs& A, const TileMatrixDev& T, const float* p
 // K, the tile side and precision and the summation; 16-bit fixed-point
 // lengths)
 void launch_forward_tiled_multi(const FwdItem* items, int n, int64_t blocks, int K, int ts,
-                                int half_tile, int comp, cudaStream_t st);
+                                int bw, int half_tile, int comp, cudaStream_t st);
 void launch_fwd_finish_multi(const FinItem* items, int n, int64_t blocks, int K, int comp,
                              cudaStream_t st);
 // plans with 16-bit fixed-point lengths (backward matrix u16, or f16 with

@@ -441,6 +441,7 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
   T.tiles_x = tiles_x;
   T.ntiles = ntiles;
   T.ts = p->fts;
+  T.bw = p->d.forward_block_warps ? p->d.forward_block_warps : 32;
   T.group_first = d_group_first;
   T.gpart = gpart;
   T.rnrun = rnrun;
@@ -544,6 +545,9 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
                       " bytes) does not fit shared memory; use a smaller "
                       "forward_tile_side, fewer slices per pass or half_gathers");
   }
+  if (d.forward_block_warps != 0 && d.forward_block_warps != 8 &&
+      d.forward_block_warps != 16 && d.forward_block_warps != 32)
+    return fail(nullptr, TG_E_ARG, "forward_block_warps must be 0, 8, 16 or 32");
   if (d.batch_streams < 0 || d.batch_streams > 2)
     return fail(nullptr, TG_E_ARG, "batch_streams must be 0, 1 or 2");
   if (d.backward_tile_width != 0 && d.backward_tile_width != 4 &&
@@ -1251,7 +1255,7 @@ void drop_states(tg_batch* b) {
 // A launch of the multi-plan kernels: kind 0 forward, 1 finish, 2 backward;
 // its items start at byte `off` of the state's item buffer.
 struct MultiLaunch {
-  int kind, branch, K, ts, half_tile, comp, dlen, pen, fh;
+  int kind, branch, K, ts, bw, half_tile, comp, dlen, pen, fh;
   size_t off;
   int n;
   int64_t blocks;
@@ -1292,7 +1296,7 @@ void multi_build(const tg_batch* b, const int* algs, const tg_params* params, in
   for (size_t i = 0; i < b->plans.size(); ++i) {
     const tg_plan* p = b->plans[i];
     const int half_tile = p->K == 16 || p->d.half_gathers;
-    branches[{p->K, p->T.ts, half_tile, p->d.compensated}].push_back((int)i);
+    branches[{p->K, p->T.ts, p->T.bw, half_tile, p->d.compensated}].push_back((int)i);
   }
   int branch = 0;
   for (auto& br : branches) {
@@ -1353,8 +1357,9 @@ void multi_build(const tg_batch* b, const int* algs, const tg_params* params, in
         l.branch = branch;
         l.K = key[0];
         l.ts = key[1];
-        l.half_tile = key[2];
-        l.comp = key[3];
+        l.bw = key[2];
+        l.half_tile = key[3];
+        l.comp = key[4];
         l.dlen = dlen;
         l.pen = pen;
         l.fh = fh;
@@ -1380,7 +1385,7 @@ void multi_issue(const std::vector<MultiLaunch>& launches, const char* d_items,
     const cudaStream_t st = branch_st[l.branch % branch_st.size()];
     if (l.kind == 0)
       launch_forward_tiled_multi(static_cast<const FwdItem*>(items), l.n, l.blocks, l.K,
-                                 l.ts, l.half_tile, l.comp, st);
+                                 l.ts, l.bw, l.half_tile, l.comp, st);
     else if (l.kind == 1)
       launch_fwd_finish_multi(static_cast<const FinItem*>(items), l.n, l.blocks, l.K, l.comp,
                               st);

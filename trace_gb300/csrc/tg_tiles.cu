@@ -34,7 +34,7 @@ namespace tg {
 
 namespace {
 
-constexpr int kBlock = 1024;      // forward: 32 warps per tile
+constexpr int kBlock = 1024;      // forward: at most 32 warps per tile block
 constexpr int kTraceBlock = 128;
 // Tiles are ts x ts pixels (TileMatrixDev::ts), kept in shared memory with
 // row stride ts + 1 (bank spread).
@@ -421,7 +421,8 @@ __device__ __forceinline__ void forward_tiled_block(const TileMatrixDev& T, int 
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g0 = T.group_first[t], g1 = T.group_first[t + 1];
-  for (int grp = g0 + sub * (kBlock / 32) + warp; grp < g1; grp += splits * (kBlock / 32)) {
+  const int nw = blockDim.x >> 5;  // warps of the block (TileMatrixDev::bw)
+  for (int grp = g0 + sub * nw + warp; grp < g1; grp += splits * nw) {
     const int slot = grp * 32 + lane;
     const int pslot = T.gpart[slot];
     const int lp = T.glp[slot];
@@ -577,7 +578,7 @@ void fwd_tiled_launch(const TileMatrixDev& T, int g, float inv_scale,
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int splits = max(1, min(16, (2 * sms + T.ntiles - 1) / T.ntiles));
-  k_forward_tiled<K, LK, H, COMP><<<T.ntiles * splits, kBlock, smem, st>>>(
+  k_forward_tiled<K, LK, H, COMP><<<T.ntiles * splits, T.bw * 32, smem, st>>>(
       T, g, inv_scale, splits, recon, part);
 }
 
@@ -744,42 +745,42 @@ void launch_fwd_finish(const IterArgs& A, const TileMatrixDev& T, const float* p
 }
 
 template <int K, int LK, bool H, bool COMP>
-static void fwd_multi_launch(const FwdItem* items, int n, int64_t blocks, int ts,
+static void fwd_multi_launch(const FwdItem* items, int n, int64_t blocks, int ts, int bw,
                              cudaStream_t st) {
   const int smem = TilePlanes<K, H>::bytes(ts);
   cudaFuncSetAttribute(k_forward_tiled_multi<K, LK, H, COMP>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  k_forward_tiled_multi<K, LK, H, COMP><<<(unsigned)blocks, kBlock, smem, st>>>(items, n);
+  k_forward_tiled_multi<K, LK, H, COMP><<<(unsigned)blocks, bw * 32, smem, st>>>(items, n);
 }
 
 // the multi-plan path serves 16-bit fixed-point lengths only
 template <int K, bool H, bool COMP>
-static void fwd_multi_kind(const FwdItem* items, int n, int64_t blocks, int ts,
+static void fwd_multi_kind(const FwdItem* items, int n, int64_t blocks, int ts, int bw,
                            cudaStream_t st) {
-  fwd_multi_launch<K, LK_U16, H, COMP>(items, n, blocks, ts, st);
+  fwd_multi_launch<K, LK_U16, H, COMP>(items, n, blocks, ts, bw, st);
 }
 
 template <int K>
-static void fwd_multi_k(const FwdItem* items, int n, int64_t blocks, int ts, int half_tile,
-                        int comp, cudaStream_t st) {
+static void fwd_multi_k(const FwdItem* items, int n, int64_t blocks, int ts, int bw,
+                        int half_tile, int comp, cudaStream_t st) {
   constexpr bool kComp = K <= 8;
   if (K == 16 || half_tile) {
-    if (kComp && comp) fwd_multi_kind<K, true, kComp>(items, n, blocks, ts, st);
-    else fwd_multi_kind<K, true, false>(items, n, blocks, ts, st);
+    if (kComp && comp) fwd_multi_kind<K, true, kComp>(items, n, blocks, ts, bw, st);
+    else fwd_multi_kind<K, true, false>(items, n, blocks, ts, bw, st);
   } else if constexpr (K != 16) {
-    if (comp) fwd_multi_kind<K, false, true>(items, n, blocks, ts, st);
-    else fwd_multi_kind<K, false, false>(items, n, blocks, ts, st);
+    if (comp) fwd_multi_kind<K, false, true>(items, n, blocks, ts, bw, st);
+    else fwd_multi_kind<K, false, false>(items, n, blocks, ts, bw, st);
   }
 }
 
 void launch_forward_tiled_multi(const FwdItem* items, int n, int64_t blocks, int K, int ts,
-                                int half_tile, int comp, cudaStream_t st) {
+                                int bw, int half_tile, int comp, cudaStream_t st) {
   switch (K) {
-    case 1: fwd_multi_k<1>(items, n, blocks, ts, half_tile, comp, st); break;
-    case 2: fwd_multi_k<2>(items, n, blocks, ts, half_tile, comp, st); break;
-    case 4: fwd_multi_k<4>(items, n, blocks, ts, half_tile, comp, st); break;
-    case 8: fwd_multi_k<8>(items, n, blocks, ts, half_tile, comp, st); break;
-    default: fwd_multi_k<16>(items, n, blocks, ts, half_tile, comp, st); break;
+    case 1: fwd_multi_k<1>(items, n, blocks, ts, bw, half_tile, comp, st); break;
+    case 2: fwd_multi_k<2>(items, n, blocks, ts, bw, half_tile, comp, st); break;
+    case 4: fwd_multi_k<4>(items, n, blocks, ts, bw, half_tile, comp, st); break;
+    case 8: fwd_multi_k<8>(items, n, blocks, ts, bw, half_tile, comp, st); break;
+    default: fwd_multi_k<16>(items, n, blocks, ts, bw, half_tile, comp, st); break;
   }
 }
 

@@ -51,6 +51,7 @@ struct Options {
   int backward_tile_width = 0;  // 8 (default), 16 or 4 pixels per tile row
   int forward_tile_side = 0;    // 64 (default), 32 or 96
   int batch_streams = 0;        // 2 (default): odd slice batches on a 2nd stream
+  int forward_block_warps = 0;  // 32 (default), 16 or 8 warps per forward tile
 };
 
 // Geometry + reconstruction (TraceMetadata). theta is copied, not owned.
@@ -90,6 +91,7 @@ class GpuTraceMetadata {
     d.backward_tile_width = opt.backward_tile_width;
     d.forward_tile_side = opt.forward_tile_side;
     d.batch_streams = opt.batch_streams;
+    d.forward_block_warps = opt.forward_block_warps;
     tg_plan* p = nullptr;
     check(tg_plan_create(&d, theta, nullptr, nullptr, &p), nullptr);
     plan_.reset(p);
