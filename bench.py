@@ -868,7 +868,8 @@ def run_batch(args, W):
             used += b
         waves.append(cur)
         iters = W["iters"]
-        e2e_s = iter_ms = setup_ms = alg_bytes = 0.0
+        e2e_s = iter_ms = setup_ms = alg_bytes = fmt_traffic = 0.0
+        ratios = ncu_traffic()
         timed_slice_iters = launches = h2d = d2h = 0
         multi = True
         ev0 = torch.cuda.Event(enable_timing=True)
@@ -906,9 +907,15 @@ def run_batch(args, W):
                     info = p.info()
                     timed_slice_iters += pr["S"] * (iters - 1)
                     K = batch_plan_kw(pr, args, tuned)["slices_per_pass"]
-                    fb, bb = kernel_bytes(info, dict(C=pr["C"], P=pr["P"], alg=pr["alg"]),
-                                          K, "u16")
+                    Wp = dict(C=pr["C"], P=pr["P"], alg=pr["alg"])
+                    fb, bb = kernel_bytes(info, Wp, K, "u16")
                     alg_bytes += (iters - 1) * info["batches"] * (fb + bb)
+                    ff, bf = format_bytes(info, Wp, K, True, args.half)
+                    fin = 4 * info["partial_slots"] * K + 4 * pr["P"] * pr["C"] * K * 2
+                    fmt_traffic += (iters - 1) * info["batches"] * (
+                        ff * ratios.get("ratio:k_forward_tiled", 1.0)
+                        + fin * ratios.get("ratio:k_fwd_finish", 1.0)
+                        + bf * ratios.get("ratio:k_backward", 1.0))
                 d2h += sum(o.numel() * 4 for o in outs)
                 launches += (iters - 1) * binfo["launches"]
                 batch.close()
@@ -950,7 +957,12 @@ def run_batch(args, W):
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak,
-                     "peak_kind": f"{peak_kind} (burst copy)", "traffic": None,
+                     "peak_kind": f"{peak_kind} (burst copy)",
+                     "traffic": fmt_traffic / (iters - 1),
+                     "traffic_basis": "DRAM bytes per step (one iteration of every wave): "
+                                      "each kernel's format bytes times its measured "
+                                      "DRAM/format ratio (profiles/ncu_traffic.json)",
+                     "frac_traffic": fmt_traffic / (iter_ms / 1e3) / 1e9 / hbm_peak,
                      "kernel": "all kernels of the batch (whole-step effective bandwidth)"},
         "clocks": clk.summary(), "gpu_launches": launches,
         "setup_ms": setup_ms, "rel_l2_vs_fp64": rel, "autotune": tune_log,
