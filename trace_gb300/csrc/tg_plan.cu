@@ -1262,7 +1262,9 @@ struct MultiLaunch {
 };
 
 // Key of iteration `it` (counted from now) of the batch: algorithms,
-// parameters and every plan's buffer parity and factor precision then.
+// parameters, every plan's buffer parity and factor precision then, and the
+// addresses of its reconstruction buffers (reallocated when a plan's layout
+// changes, which the captured work items must follow).
 std::string multi_key(const tg_batch* b, const int* algs, const tg_params* params, int it) {
   std::string k;
   for (size_t i = 0; i < b->plans.size(); ++i) {
@@ -1273,6 +1275,7 @@ std::string multi_key(const tg_batch* b, const int* algs, const tg_params* param
     const tg_params prm = params ? params[i] : tg_params{};
     k.append(reinterpret_cast<const char*>(&algs[i]), sizeof(int));
     k.append(reinterpret_cast<const char*>(&prm), sizeof(prm));
+    k.append(reinterpret_cast<const char*>(p->d_recon), sizeof(p->d_recon));
     k.push_back((char)(cur | (hf << 1)));
   }
   return k;
