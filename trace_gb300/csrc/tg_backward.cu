@@ -19,7 +19,7 @@ void launch_backward_multi(const BackItem* items, int n, int64_t blocks, int K,
   }
 }
 
-int64_t backward_blocks(const IterArgs& A) { return backward_block_count(A.M); }
+int64_t backward_blocks(const IterArgs& A) { return (A.M.ntiles + kWarps - 1) / kWarps; }
 
 void launch_backward(const IterArgs& A, int batch, const float* recon_cur,
                      float* recon_next, const float* upd, float* rep_num,

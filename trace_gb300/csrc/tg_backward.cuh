@@ -161,19 +161,6 @@ __device__ __forceinline__ void accumulate(float (&acc)[K], const float (&rf)[K]
   }
 }
 
-// A block's 8 warps take a bw x bh arrangement of pixel tiles (2 x 4 of
-// 16x2 or 8x4 tiles, 4 x 2 of 4x8 tiles: 32x8 or 16x16 pixels) rather than
-// 8 tiles of one row: at one angle the rays through a squarer block span a
-// narrower detector window, so its warps share more factor lines in L1.
-__host__ __device__ __forceinline__ int block_tiles_w(const MatrixDev& M) {
-  return M.tw_shift == 2 ? 4 : 2;
-}
-__host__ __device__ __forceinline__ int64_t backward_block_count(const MatrixDev& M) {
-  const int bw = block_tiles_w(M), bh = kWarps / bw;
-  const int tiles_y = M.ntiles / M.tiles_x;
-  return (int64_t)((M.tiles_x + bw - 1) / bw) * ((tiles_y + bh - 1) / bh);
-}
-
 // Resident blocks per SM for each variant: compensated sums keep two more
 // K-float arrays per thread (the quad's sum and the Kahan correction).
 template <int K, bool COMP>
@@ -196,14 +183,10 @@ __device__ __forceinline__ void backward_block(const IterArgs& A, int batch, int
   const int g = G.C;
   const int64_t g2 = (int64_t)g * g;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int bw = block_tiles_w(A.M), bh = kWarps / bw;
-  const int nbx = (A.M.tiles_x + bw - 1) / bw;
-  const int tx = (block % nbx) * bw + warp % bw, ty = (block / nbx) * bh + warp / bw;
-  const bool tile_ok = tx < A.M.tiles_x && ty < A.M.ntiles / A.M.tiles_x;
-  const int tile = ty * A.M.tiles_x + tx;
+  const int tile = block * kWarps + warp;
   int x, y;
   tile_pixel(tile, lane, A.M.tiles_x, A.M.tw_shift, &x, &y);
-  const bool valid = tile_ok && x < g && y < g;
+  const bool valid = tile < A.M.ntiles && x < g && y < g;
   const int64_t p = (int64_t)y * g + x;
   const float xf = (float)x, yf = (float)y;
   const int fslot0 = batch * K + A.fshift;  // multiple of K
@@ -427,7 +410,7 @@ void back_multi(const BackItem* items, int n, int64_t blocks, int dlen_kind, int
 template <int K, int LK>
 void back_launch(const IterArgs& A, int batch, const float* cur, float* next,
                  const float* upd, float* rep_num, int epi, cudaStream_t st) {
-  const int blocks = (int)backward_block_count(A.M);
+  const int blocks = (A.M.ntiles + kWarps - 1) / kWarps;
   const bool pen = A.alg >= 2;
 #define TG_BACK(E, PN, FH, CP)                                                        \
   k_backward<K, LK, E, PN, FH, CP><<<blocks, kBlock, 0, st>>>(A, batch, cur, next, upd, \
