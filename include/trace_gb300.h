@@ -141,8 +141,9 @@ typedef struct {
                               backprojection: 8 (8x4 tiles; 0 selects it),
                               16 (16x2) or 4 (4x8); backward_staged needs 8 */
   int forward_tile_side;   /* forward_tiles: side of the shared-memory
-                              reconstruction tiles, 32, 64 (0 selects it) or
-                              96; the tile of slices_per_pass slices must fit
+                              reconstruction tiles, 32, 48, 64 (0 selects
+                              it), 80 or 96; the tile of slices_per_pass
+                              slices must fit
                               shared memory (96 needs half_gathers and at
                               most 8 slices per pass) */
   int batch_streams;       /* forward_tiles with two or more slice batches:

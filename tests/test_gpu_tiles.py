@@ -273,10 +273,10 @@ def test_backward_tile_shapes_are_bit_identical(kw, alg):
     assert np.array_equal(bits(outs[2]), bits(outs[0]))
 
 
-@pytest.mark.parametrize("ts", [32, 96])
+@pytest.mark.parametrize("ts", [32, 48, 80, 96])
 @pytest.mark.parametrize("alg", ["sirt", "mlem", "pml"])
 def test_forward_tile_sides(ts, alg):
-    """Forward tiles of 32 or 96 pixels regroup each ray's sum by tile runs:
+    """Forward tiles of 32 to 96 pixels regroup each ray's sum by tile runs:
     within 1e-6 of the 64-pixel tiles with FP32 operands, and the benchmark
     configuration stays within 1e-4 of the FP64 oracle."""
     C, P, S, it = 200, 150, 8, 5
@@ -310,10 +310,11 @@ def test_forward_tile_that_does_not_fit_is_rejected():
         tg.Plan(8, 8, 100, theta_uniform(8), slices_per_pass=8, mode="fast",
                 forward_tiles=True, forward_tile_side=96)  # f32 tile: 298 KB
     assert e.value.status == 1
-    with pytest.raises(tg.TraceError) as e:
-        tg.Plan(8, 1, 100, theta_uniform(8), mode="fast", forward_tiles=True,
-                forward_tile_side=48)
-    assert e.value.status == 1
+    for side in (40, 112):  # not a multiple of 16; beyond the one-byte step
+        with pytest.raises(tg.TraceError) as e:
+            tg.Plan(8, 1, 100, theta_uniform(8), mode="fast", forward_tiles=True,
+                    forward_tile_side=side)
+        assert e.value.status == 1
 
 
 @pytest.mark.parametrize("warps", [8, 16])

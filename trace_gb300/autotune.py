@@ -35,7 +35,7 @@ DEFAULT_SPACE = {
 
 # refined one at a time from the best configuration of DEFAULT_SPACE
 REFINE_SPACE = {
-    "forward_tile_side": (32, 64, 96),     # forward_tiles: shared-memory tile side
+    "forward_tile_side": (32, 48, 64, 80, 96),  # forward_tiles: shared-memory tile side
     "backward_tile_width": (4, 8, 16),     # backprojection tiles 4x8, 8x4, 16x2
     "forward_block_warps": (8, 16, 32),    # forward_tiles: runs in flight per tile
 }

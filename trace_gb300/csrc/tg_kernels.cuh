@@ -48,8 +48,8 @@ struct MatrixDev {
 
 // Tile-staged forward matrix (tg_tiles.cu): per ts x ts tile, groups of 32
 // runs (consecutive segments of one ray inside the tile), lane = run. The
-// tile side ts is a plan choice (32, 64 or 96; a step inside a tile is one
-// signed byte dx + dy * (ts + 1), so ts + 1 <= 127).
+// tile side ts is a plan choice (32 to 96 in steps of 16; a step inside a
+// tile is one signed byte dx + dy * (ts + 1), so ts + 1 <= 127).
 constexpr int kTileSide = 64;
 
 __device__ __forceinline__ int tile_of_pixel(int ix, int iy, int tiles_x, int ts) {

@@ -530,9 +530,11 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
     return fail(nullptr, TG_E_ARG,
                 "compensated needs fast mode, forward_tiles, the L1 backprojection and "
                 "at most 8 slices per pass");
-  if (d.forward_tile_side != 0 && d.forward_tile_side != 32 && d.forward_tile_side != 64 &&
-      d.forward_tile_side != 96)
-    return fail(nullptr, TG_E_ARG, "forward_tile_side must be 0, 32, 64 or 96");
+  // tile sides: multiples of 16 up to 96 (a step's shared-memory index
+  // change dx + dy * (side + 1) must fit a signed byte)
+  if (d.forward_tile_side != 0 &&
+      (d.forward_tile_side < 32 || d.forward_tile_side > 96 || d.forward_tile_side % 16))
+    return fail(nullptr, TG_E_ARG, "forward_tile_side must be 0, 32, 48, 64, 80 or 96");
   if (d.forward_tiles) {
     // the shared-memory tile: side x (side + 1) pixels of slices_per_pass
     // values, halves with half_gathers (and always at 16 slices per pass)
