@@ -41,6 +41,14 @@
  * (batch_streams) and joins it back into that stream before returning, so
  * callers see stream order as if one stream did all the work. Calls on one
  * plan are not thread-safe; distinct plans are independent.
+ *
+ * Host buffers (on_device = 0): a page-locked buffer (cudaHostAlloc,
+ * cudaMallocHost, or cudaHostRegister'ed and mapped) is read or written in
+ * place by the kernels that convert between the reference layout and the
+ * device layout, across the CPU-GPU link, with no device staging copy; a
+ * pageable buffer goes through a device staging buffer. Either way a call
+ * that takes a host buffer returns after it has read (uploads) or written
+ * (downloads) it.
  */
 #ifndef TRACE_GB300_H
 #define TRACE_GB300_H
@@ -115,10 +123,12 @@ typedef struct {
                              factor - 1 - halving the bytes of both gathers;
                              the backward matrix then stores its lengths as
                              halves (16-bit storages). The first iteration
-                             after tg_reset_recon / tg_set_recon keeps FP32
-                             factors (they start far from 1, where a half of
-                             factor - 1 is least precise). tg_reduce keeps
-                             FP32 factors (half tile) */
+                             after tg_reset_recon / tg_set_recon stores
+                             halves of the factors themselves (they start
+                             anywhere between 0 and their largest value,
+                             where a half of factor - 1 loses the small
+                             ones). tg_reduce keeps FP32 factors (half
+                             tile) */
   int forward_on_the_fly; /* not with FP64 mode: no ray-ordered forward matrix
                              is stored; the forward projections that would
                              read it (tg_iterate, tg_reduce and

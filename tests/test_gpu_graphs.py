@@ -94,7 +94,7 @@ def test_batch_multi_plan_launches_match_individual_plans():
     """Fast tile-staged plans with 16-bit lengths advance together through the
     multi-plan launches (one per kernel variant and slice-batch round, blocks
     walking every plan's work): bit-identical to each plan iterated alone,
-    from a fresh reconstruction (FP32-factor first iteration) on, across
+    from a fresh reconstruction (first iteration: halves of the factors) on, across
     calls (buffer parity), with far fewer launches than per-plan kernels."""
     def mk(i, spec):
         C, P, S, alg, K, half, comp = spec

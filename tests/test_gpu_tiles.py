@@ -67,7 +67,7 @@ def test_half_gathers_against_fp64(alg, K, S):
     16-bit lengths. Small grids converge from far away in few iterations, the
     loosest case for half factors (rel-L2 bound 1e-4 here; the 2048^2 x 1500
     workload's 30-iteration error is measured by the benchmark). The first
-    iteration keeps FP32 factors."""
+    iteration stores halves of the factors, later ones of factor - 1."""
     C, P, it = 96, 72, 6
     th = theta_uniform(P)
     tabs = O.angle_table(th)

@@ -120,6 +120,19 @@ def _is_device(a):
     return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
 
 
+def _host_out(out, shape):
+    """A new float32 host array of `shape`, or the caller's host buffer (numpy
+    array or CPU tensor; page-locked memory is written by the kernels in
+    place) after checking that it is C-contiguous float32 of that shape."""
+    if out is None:
+        return np.empty(shape, np.float32)
+    view = out.numpy() if hasattr(out, "numpy") else out
+    if (not isinstance(view, np.ndarray) or view.dtype != np.float32
+            or view.shape != tuple(shape) or not view.flags.c_contiguous):
+        raise ValueError(f"out must be a C-contiguous float32 array of shape {tuple(shape)}")
+    return out
+
+
 def default_params(alg: str, beta=None, beta1=1.0, delta=1.0, delta1=1.0,
                    regw=1.0) -> Params:
     """Reference defaults: PML beta 10 (pml_main.cc:20), APMLR beta0=10,
@@ -257,14 +270,7 @@ class Plan:
             self._chk(self._lib.tg_get_recon(self._h, self._alg(alg), _ptr(out), 1))
             return out
         n = self.S + 2 * self.halo(alg)
-        if out is None:
-            out = np.empty((n, self.C, self.C), np.float32)
-        else:
-            view = out.numpy() if hasattr(out, "numpy") else out
-            if (not isinstance(view, np.ndarray) or view.dtype != np.float32
-                    or view.shape != (n, self.C, self.C) or not view.flags.c_contiguous):
-                raise ValueError(f"out must be a C-contiguous float32 array of shape "
-                                 f"{(n, self.C, self.C)}")
+        out = _host_out(out, (n, self.C, self.C))
         self._chk(self._lib.tg_get_recon(self._h, self._alg(alg), _ptr(out), 0))
         return out
 
@@ -277,8 +283,10 @@ class Plan:
         p = params if params is not None else default_params(alg)
         self._chk(self._lib.tg_reduce(self._h, self._alg(alg), C.byref(p)))
 
-    def get_replica(self, alg):
-        out = np.empty((self.S, 2 * self.C * self.C), np.float32)
+    def get_replica(self, alg, out=None):
+        """The reduction replica, [S][2 C C] (per pixel: value, weight), into
+        `out` (a host array or CPU tensor of that shape) or a new array."""
+        out = _host_out(out, (self.S, 2 * self.C * self.C))
         self._chk(self._lib.tg_get_replica(self._h, self._alg(alg), _ptr(out), 0))
         return out
 
@@ -304,7 +312,7 @@ class Plan:
         if out is not None and _is_device(out):
             self._chk(self._lib.tg_forward_project(self._h, self._alg(alg), C.byref(p), _ptr(out), 1))
             return out
-        out = np.empty((self.P, self.S, self.C), np.float32)
+        out = _host_out(out, (self.P, self.S, self.C))
         self._chk(self._lib.tg_forward_project(self._h, self._alg(alg), C.byref(p), _ptr(out), 0))
         return out
 

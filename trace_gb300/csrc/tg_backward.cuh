@@ -137,8 +137,9 @@ __device__ __forceinline__ void load_hwords(uint32_t (&w)[K / 2], const __half* 
   }
 }
 
-// FH: the factors are halves (factor - 1), see k_fwd_finish; the missing
-// sum of lengths is the pixel's total length W, added in the epilogue.
+// FH: the factors are halves (factor - 1) or (factor), see k_fwd_finish; in
+// the first case the missing sum of lengths is the pixel's total length W,
+// added in the epilogue.
 template <int K, bool EXACT, bool PEN, bool FH>
 __device__ __forceinline__ void accumulate(float (&acc)[K], const float (&rf)[K],
                                            float l, const float* ub) {
@@ -324,8 +325,10 @@ __device__ __forceinline__ void backward_block(const IterArgs& A, int batch, int
     accumulate<K, EXACT, PEN, FH>(acc, rf, l, ub);
   });
   if constexpr (FH) {
+    if (A.half_factors == FACT_HALF_M1) {
 #pragma unroll
-    for (int j = 0; j < K; ++j) acc[j] += Wp;
+      for (int j = 0; j < K; ++j) acc[j] += Wp;
+    }
   }
   if (PEN && !EXACT) {  // the reconstruction factor, applied once per pixel
     const Vec<K> v = load_vec<K>(fsrc);

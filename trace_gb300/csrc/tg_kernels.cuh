@@ -52,8 +52,23 @@ struct MatrixDev {
 // tile is one signed byte dx + dy * (ts + 1), so ts + 1 <= 127).
 constexpr int kTileSide = 64;
 
-__device__ __forceinline__ int tile_of_pixel(int ix, int iy, int tiles_x, int ts) {
-  return (iy / ts) * tiles_x + ix / ts;
+// Division by the tile side without an integer divide (the construction
+// kernels take it for every segment): q = umulhi(v, m), m = ceil(2^32 / ts),
+// exact for 0 <= v < 2^32 / ts, because v * (m * ts - 2^32) < 2^32 keeps
+// the error of v * m / 2^32 below 1 / ts, the smallest distance from v / ts
+// up to the next integer.
+struct TileDiv {
+  int ts;
+  uint32_t m;
+};
+inline TileDiv make_tile_div(int ts) {
+  return TileDiv{ts, 0xFFFFFFFFu / (uint32_t)(ts > 0 ? ts : 1) + 1u};
+}
+__device__ __forceinline__ int tdiv(int v, TileDiv d) {
+  return (int)__umulhi((uint32_t)v, d.m);
+}
+__device__ __forceinline__ int tile_of_pixel(int ix, int iy, int tiles_x, TileDiv d) {
+  return tdiv(iy, d) * tiles_x + tdiv(ix, d);
 }
 
 // A 4-bit step code holds (dx, dy) in {0,1} x {-1,0,1}. The reference's
@@ -110,9 +125,8 @@ struct IterArgs {
   PenaltyWeights pw;
   // 16-bit gather operands (fast mode, set per launch sequence):
   // half_tile - the tile-staged forward keeps its shared-memory tile as
-  //             halves; half_factors - the per-ray factors are stored as
-  //             halves of (factor - 1) (ratio algorithms) and the
-  //             backprojection adds the per-pixel total length back
+  //             halves; half_factors - storage of the per-ray ratio
+  //             factors (FACT_*)
   int half_tile;
   int half_factors;
   // compensated (Kahan) summation of the ray and pixel sums (fast mode,
@@ -131,6 +145,19 @@ struct FwdItem {
   float inv_scale;
   int64_t first;
 };
+// Storage of the per-ray ratio factors between the forward finish and the
+// backprojection. FACT_HALF_M1: halves of (factor - 1), exact to a half's
+// precision relative to the factor's distance from 1, so the steady state
+// (factors near 1) loses least; the backprojection adds the pixel's total
+// length back. FACT_HALF: halves of the factor itself, a half's relative
+// precision whatever the factor, for the first iteration after a reset,
+// where factors lie anywhere between 0 and their largest value.
+enum { FACT_F32 = 0, FACT_HALF_M1 = 1, FACT_HALF = 2 };
+
+__host__ __device__ inline float factor_offset(int half_factors) {
+  return half_factors == FACT_HALF_M1 ? 1.f : 0.f;
+}
+
 struct FinItem {
   const int* rnrun;
   const int* pbase;
@@ -141,7 +168,7 @@ struct FinItem {
   int64_t nrays;
   int64_t first;        // 256 rays a block
   int out_mode;
-  int fh;               // factors stored as halves of (factor - 1)
+  int fh;               // factor storage (FACT_*)
 };
 struct BackItem {
   IterArgs A;

@@ -61,8 +61,8 @@ struct tg_plan {
   float* d_recon[2] = {nullptr, nullptr};
   int cur = 0;
   // fused iterations since the reconstruction was last reset or uploaded:
-  // with half_gathers the first one keeps FP32 factors (factors start far
-  // from 1, where a half of factor - 1 loses the most)
+  // with half_gathers the first one stores halves of the factors, later ones
+  // halves of factor - 1 (factor_storage)
   int64_t iters_done = 0;
   float* d_upd = nullptr;
   float* d_rep = nullptr;
@@ -168,6 +168,32 @@ int quadrant_of(float t) {
 int halo_of(int alg) { return alg == TG_APMLR ? 1 : 0; }
 
 bool valid_alg(int alg) { return alg >= TG_SIRT && alg <= TG_APMLR; }
+
+// Device address through which kernels read or write the `n` floats of
+// caller host memory at `ptr` in place, or nullptr. Page-locked host memory
+// (cudaHostAlloc / cudaMallocHost, or registered as mapped) is addressable
+// by kernels across GB300's CPU-GPU link, so the layout kernels pack from
+// and unpack into it directly: no device staging buffer to allocate and no
+// separate copy. Both ends of the range must be page-locked and map to one
+// linear device range; anything else (pageable memory) is staged.
+float* mapped_host(const void* ptr, size_t n) {
+  if (n == 0) return nullptr;
+  const char* first = static_cast<const char*>(ptr);
+  const char* last = first + (n - 1) * sizeof(float);
+  cudaPointerAttributes a{}, b{};
+  if (cudaPointerGetAttributes(&a, first) != cudaSuccess ||
+      cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost ||
+      !a.devicePointer || !b.devicePointer)
+    return nullptr;
+  if (static_cast<char*>(b.devicePointer) - static_cast<char*>(a.devicePointer) !=
+      last - first)
+    return nullptr;
+  return static_cast<float*>(a.devicePointer);
+}
 
 // Stage host data through one reusable device buffer.
 int stage(tg_plan* p, size_t n) {
@@ -964,7 +990,7 @@ static int set_sinogram(tg_plan* p, const float* sino, int on_device,
   TG_CUDA(p, cudaMemsetAsync(p->d_sino, 0,
                              (size_t)p->nb * p->R * p->K * sizeof(float), p->st));
   const float* src = sino;
-  if (!on_device) {
+  if (!on_device && !(src = mapped_host(sino, n))) {
     TG_TRY(stage(p, n));
     TG_CUDA(p, cudaMemcpyAsync(p->d_stage, sino, n * sizeof(float),
                                cudaMemcpyHostToDevice, p->st));
@@ -973,6 +999,8 @@ static int set_sinogram(tg_plan* p, const float* sino, int on_device,
   launch_sino_pack(src, p->d_sino, p->P, p->S, p->C, p->K, apply_abs, clip, clip_min,
                    p->st);
   TG_CUDA(p, cudaGetLastError());
+  // a host sinogram has been read when the call returns
+  if (!on_device) TG_CUDA(p, cudaStreamSynchronize(p->st));
   p->have_sino = true;
   return TG_OK;
 }
@@ -1007,21 +1035,25 @@ int tg_set_recon(tg_plan* p, int alg, const float* recon, int on_device) {
   const int nuser = p->S + 2 * p->halo;
   const size_t n = (size_t)nuser * p->g2;
   const float* src = recon;
-  if (!on_device) {
+  if (!on_device && !(src = mapped_host(recon, n))) {
     TG_TRY(stage(p, n));
     TG_CUDA(p, cudaMemcpyAsync(p->d_stage, recon, n * sizeof(float),
                                cudaMemcpyHostToDevice, p->st));
     src = p->d_stage;
   }
-  for (int b = 0; b < 2; ++b) {
-    if (p->fp64)
-      launch_convert(src, as_f64(p->d_recon[b]) + (int64_t)(p->vshift - p->halo) * p->g2,
-                     (int64_t)n, p->st);
-    else
-      launch_recon_pack(src, p->d_recon[b], nuser, (int)p->g2, p->K,
-                        p->vshift - p->halo, p->nslots, p->st);
-  }
+  // the source is read once; the second buffer is a device copy of the first
+  if (p->fp64)
+    launch_convert(src, as_f64(p->d_recon[0]) + (int64_t)(p->vshift - p->halo) * p->g2,
+                   (int64_t)n, p->st);
+  else
+    launch_recon_pack(src, p->d_recon[0], nuser, (int)p->g2, p->K,
+                      p->vshift - p->halo, p->nslots, p->st);
   TG_CUDA(p, cudaGetLastError());
+  TG_CUDA(p, cudaMemcpyAsync(p->d_recon[1], p->d_recon[0],
+                             (size_t)p->nslots * p->g2 * (p->fp64 ? 8 : 4),
+                             cudaMemcpyDeviceToDevice, p->st));
+  // a host reconstruction has been read when the call returns
+  if (!on_device) TG_CUDA(p, cudaStreamSynchronize(p->st));
   return TG_OK;
 }
 
@@ -1031,9 +1063,14 @@ int tg_get_recon(tg_plan* p, int alg, float* recon, int on_device) {
   const int nuser = p->S + 2 * p->halo;
   const size_t n = (size_t)nuser * p->g2;
   float* dst = recon;
+  float* mapped = on_device ? nullptr : mapped_host(recon, n);
   if (!on_device) {
-    TG_TRY(stage(p, n));
-    dst = p->d_stage;
+    if (mapped) {
+      dst = mapped;
+    } else {
+      TG_TRY(stage(p, n));
+      dst = p->d_stage;
+    }
   }
   if (p->fp64)
     launch_narrow(as_f64(p->d_recon[p->cur]) + (int64_t)(p->vshift - p->halo) * p->g2,
@@ -1042,7 +1079,9 @@ int tg_get_recon(tg_plan* p, int alg, float* recon, int on_device) {
     launch_recon_unpack(p->d_recon[p->cur], dst, nuser, (int)p->g2, p->K,
                         p->vshift - p->halo, p->st);
   TG_CUDA(p, cudaGetLastError());
-  if (!on_device) {
+  if (mapped) {
+    TG_CUDA(p, cudaStreamSynchronize(p->st));
+  } else if (!on_device) {
     TG_CUDA(p, cudaMemcpyAsync(recon, p->d_stage, n * sizeof(float),
                                cudaMemcpyDeviceToHost, p->st));
     TG_CUDA(p, cudaStreamSynchronize(p->st));
@@ -1078,10 +1117,16 @@ static int run_forward(tg_plan* p, const IterArgs& A0, int b, int out_mode,
   return TG_OK;
 }
 
-// Whether this plan's next fused iteration stores its ratio factors as
-// halves of (factor - 1): half_gathers plans from their second iteration on.
+// Storage of the ratio factors of a fused iteration on a plan that has run
+// `done` iterations since its reset (FACT_*): on half_gathers plans halves
+// of the factor in the first iteration, of (factor - 1) from the second on.
+static int factor_storage(const tg_plan* p, int mode, int64_t done) {
+  if (!(p->tiles && p->d.half_gathers && mode == FWD_RATIO)) return FACT_F32;
+  return done >= 1 ? FACT_HALF_M1 : FACT_HALF;
+}
+
 static int half_factors_next(const tg_plan* p, int mode) {
-  return p->tiles && p->d.half_gathers && mode == FWD_RATIO && p->iters_done >= 1;
+  return factor_storage(p, mode, p->iters_done);
 }
 
 // Launches of one fused iteration on the plan's stream (buffers by p->cur;
@@ -1273,7 +1318,7 @@ std::string multi_key(const tg_batch* b, const int* algs, const tg_params* param
     const tg_plan* p = b->plans[i];
     const int mode = algs[i] == TG_SIRT ? FWD_SIRT : FWD_RATIO;
     const int cur = p->cur ^ (it & 1);
-    const int hf = p->tiles && p->d.half_gathers && mode == FWD_RATIO && p->iters_done + it >= 1;
+    const int hf = factor_storage(p, mode, p->iters_done + it);
     const tg_params prm = params ? params[i] : tg_params{};
     k.append(reinterpret_cast<const char*>(&algs[i]), sizeof(int));
     k.append(reinterpret_cast<const char*>(&prm), sizeof(prm));
@@ -1317,7 +1362,7 @@ void multi_build(const tg_batch* b, const int* algs, const tg_params* params, in
         if (r >= p->nb) continue;
         const int mode = algs[i] == TG_SIRT ? FWD_SIRT : FWD_RATIO;
         const int cur = p->cur ^ (it & 1);
-        const int hf = p->d.half_gathers && mode == FWD_RATIO && p->iters_done + it >= 1;
+        const int hf = factor_storage(p, mode, p->iters_done + it);
         IterArgs A = make_args(p, algs[i], params ? &params[i] : nullptr);
         A.half_tile = p->d.half_gathers;
         A.half_factors = hf;
@@ -1348,7 +1393,8 @@ void multi_build(const tg_batch* b, const int* algs, const tg_params* params, in
         k.next = p->d_recon[cur ^ 1];
         k.upd = p->d_upd;
         k.first = backward_blocks(A);
-        back[{A.M.dlen_kind, algs[i] >= TG_PML, hf}].push_back(k);
+        // both half storages share one kernel (each item carries its own)
+        back[{A.M.dlen_kind, algs[i] >= TG_PML, hf != FACT_F32}].push_back(k);
       }
       auto emit = [&](int kind, auto& items, int dlen, int pen, int fh) {
         int64_t total = 0;
@@ -1665,13 +1711,20 @@ int tg_get_replica(tg_plan* p, int alg, float* replica, int on_device) {
   if (!p->d_rep) return fail(p, TG_E_STATE, "no replica: call tg_reduce first");
   const size_t n = (size_t)p->S * p->g2 * 2;
   float* dst = replica;
+  float* mapped = on_device ? nullptr : mapped_host(replica, n);
   if (!on_device) {
-    TG_TRY(stage(p, n));
-    dst = p->d_stage;
+    if (mapped) {
+      dst = mapped;
+    } else {
+      TG_TRY(stage(p, n));
+      dst = p->d_stage;
+    }
   }
   launch_replica_interleave(p->d_rep, p->d_W, dst, p->S, (int)p->g2, p->st);
   TG_CUDA(p, cudaGetLastError());
-  if (!on_device) {
+  if (mapped) {
+    TG_CUDA(p, cudaStreamSynchronize(p->st));
+  } else if (!on_device) {
     TG_CUDA(p, cudaMemcpyAsync(replica, p->d_stage, n * sizeof(float),
                                cudaMemcpyDeviceToHost, p->st));
     TG_CUDA(p, cudaStreamSynchronize(p->st));
@@ -1740,14 +1793,16 @@ int tg_forward_project(tg_plan* p, int alg, const tg_params* prm, float* sim,
   TG_TRY(check_layout(p, alg));
   const size_t packed = (size_t)p->nb * p->R * p->K;
   const size_t n = (size_t)p->P * p->S * p->C;
-  TG_TRY(stage(p, packed + (on_device ? 0 : n)));
+  float* mapped = on_device ? nullptr : mapped_host(sim, n);
+  const bool staged = !on_device && !mapped;
+  TG_TRY(stage(p, packed + (staged ? n : 0)));
   const IterArgs A = make_args(p, alg, prm);
   for (int b = 0; b < p->nb; ++b)
     run_forward(p, A, b, FWD_SIM, p->d_stage + (int64_t)b * p->R * p->K);
-  float* dst = on_device ? sim : p->d_stage + packed;
+  float* dst = on_device ? sim : mapped ? mapped : p->d_stage + packed;
   launch_sino_unpack(p->d_stage, dst, p->P, p->S, p->C, p->K, p->st);
   TG_CUDA(p, cudaGetLastError());
-  if (!on_device)
+  if (staged)
     TG_CUDA(p, cudaMemcpyAsync(sim, dst, n * sizeof(float), cudaMemcpyDeviceToHost, p->st));
   TG_CUDA(p, cudaStreamSynchronize(p->st));
   return TG_OK;

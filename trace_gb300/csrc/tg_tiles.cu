@@ -46,8 +46,8 @@ constexpr int kTraceBlock = 128;
 // first step, steps past a run's end, empty lanes) holds it, with a zero
 // length. Per lane and chunk the 8 bytes are one 8-byte word pair.
 
-__device__ __forceinline__ int tile_of(int ix, int iy, int tiles_x, int ts) {
-  return tile_of_pixel(ix, iy, tiles_x, ts);
+__device__ __forceinline__ int tile_of(int ix, int iy, int tiles_x, TileDiv d) {
+  return tile_of_pixel(ix, iy, tiles_x, d);
 }
 
 // ---- construction (runs per ray are counted by k_trace_count) ----------------
@@ -116,7 +116,7 @@ __device__ __forceinline__ unsigned long long run_key(RunKey rk, int t, int len,
 
 template <int SRC>
 __global__ void __launch_bounds__(kTraceBlock)
-    k_runs_emit(DevGeom G, MatrixDev M, int tiles_x, int ts, RunKey rk,
+    k_runs_emit(DevGeom G, MatrixDev M, int tiles_x, TileDiv td, RunKey rk,
                 const int64_t* ray_run_off, unsigned long long* key, int* val,
                 uint16_t* run_lp, uint16_t* run_len, int* tile_count) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(kTraceBlock)
     }
   };
   ray_segments<SRC, false>(G, M, r, [&](int, int ix, int iy, float, uint16_t) {
-    const int t = tile_of(ix, iy, tiles_x, ts);
+    const int t = tile_of(ix, iy, tiles_x, td);
     const bool step_ok = unit_step(ix, iy, px, py);
     px = ix;
     py = iy;
@@ -141,7 +141,8 @@ __global__ void __launch_bounds__(kTraceBlock)
       cur = t;
       len = 0;
       val[i] = (int)i;
-      run_lp[i] = (uint16_t)((iy % ts) * ts + ix % ts);
+      const int ts = td.ts;
+      run_lp[i] = (uint16_t)((iy - tdiv(iy, td) * ts) * ts + ix - tdiv(ix, td) * ts);
       atomicAdd(&tile_count[t], 1);
     }
     ++len;
@@ -179,7 +180,7 @@ __global__ void k_runs_group(RunKey rk, const unsigned long long* skey, const in
 
 template <bool L16, int SRC>
 __global__ void __launch_bounds__(kTraceBlock)
-    k_runs_fill(DevGeom G, MatrixDev M, int tiles_x, int ts, const int64_t* ray_run_off,
+    k_runs_fill(DevGeom G, MatrixDev M, int tiles_x, TileDiv td, const int64_t* ray_run_off,
                 const int* run_slot, const int64_t* gseg_off,
                 const int64_t* gcode_off, void* tlen, uint32_t* tcode) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(kTraceBlock)
     }
   };
   ray_segments<SRC, L16>(G, M, r, [&](int, int ix, int iy, float l, uint16_t code) {
-    const int t = tile_of(ix, iy, tiles_x, ts);
+    const int t = tile_of(ix, iy, tiles_x, td);
     if (t != cur || !unit_step(ix, iy, px, py)) {
       flush();
       ++i;
@@ -235,7 +236,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       lbase = gseg_off[grp] + lane * 8;
       cbase = gcode_off[grp] + lane * 2;
     } else {
-      const uint32_t b = (uint32_t)((ix - px) + (iy - py) * (ts + 1)) & 0xffu;
+      const uint32_t b = (uint32_t)((ix - px) + (iy - py) * (td.ts + 1)) & 0xffu;
       if ((s & 7) < 4) w0 |= b << (8 * (s & 3));
       else w1 |= b << (8 * (s & 3));
     }
@@ -495,14 +496,15 @@ __global__ void __launch_bounds__(kBlock)
 
 // A ray's partial sums (its runs' slots, in path order) -> per-ray factor,
 // as k_forward's epilogue. FH (ratio factors only): the factor is stored as
-// the half (ray/sim - 1).
+// the half (ray/sim - fofs), fofs = factor_offset(storage).
 template <int K, bool FH, bool COMP>
 __device__ __forceinline__ void fwd_finish_ray(int64_t r, const int* __restrict__ rnrun,
                                                const int* __restrict__ pbase,
                                                const float* __restrict__ ra2,
                                                const float* __restrict__ part,
                                                const float* __restrict__ sino,
-                                               float* __restrict__ out, int out_mode) {
+                                               float* __restrict__ out, int out_mode,
+                                               float fofs) {
   Vec<K> s;
   float cmp[K];
 #pragma unroll
@@ -535,7 +537,7 @@ __device__ __forceinline__ void fwd_finish_ray(int64_t r, const int* __restrict_
   }
   if constexpr (FH) {
 #pragma unroll
-    for (int j = 0; j < K; ++j) o.v[j] -= 1.f;
+    for (int j = 0; j < K; ++j) o.v[j] -= fofs;
     store_hvec<K>(reinterpret_cast<__half*>(out) + r * K, o);
   } else {
     store_vec<K>(out + r * K, o);
@@ -548,9 +550,10 @@ __global__ void k_fwd_finish(int64_t nrays, const int* __restrict__ rnrun,
                              const float* __restrict__ ra2,
                              const float* __restrict__ part,
                              const float* __restrict__ sino,
-                             float* __restrict__ out, int out_mode) {
+                             float* __restrict__ out, int out_mode, float fofs) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < nrays) fwd_finish_ray<K, FH, COMP>(r, rnrun, pbase, ra2, part, sino, out, out_mode);
+  if (r < nrays)
+    fwd_finish_ray<K, FH, COMP>(r, rnrun, pbase, ra2, part, sino, out, out_mode, fofs);
 }
 
 // Many plans' finishes in one launch: block -> work item, 256 rays a block.
@@ -559,12 +562,12 @@ __global__ void k_fwd_finish_multi(const FinItem* __restrict__ items, int nitems
   const FinItem& it = items[item_of(items, nitems, blockIdx.x)];
   const int64_t r = (int64_t)(blockIdx.x - it.first) * blockDim.x + threadIdx.x;
   if (r >= it.nrays) return;
-  if (it.fh)
+  if (it.fh != FACT_F32)
     fwd_finish_ray<K, true, COMP>(r, it.rnrun, it.pbase, it.ra2, it.part, it.sino, it.out,
-                                  it.out_mode);
+                                  it.out_mode, factor_offset(it.fh));
   else
     fwd_finish_ray<K, false, COMP>(r, it.rnrun, it.pbase, it.ra2, it.part, it.sino, it.out,
-                                   it.out_mode);
+                                   it.out_mode, 0.f);
 }
 
 template <int K, int LK, bool H, bool COMP>
@@ -628,18 +631,19 @@ void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts,
                       cudaStream_t st) {
   const int64_t R = (int64_t)G.P * G.C;
   const int blocks = blocks_for(R, kTraceBlock);
+  const TileDiv td = make_tile_div(ts);
   switch (seg_source(M)) {
     case kSrcDelta:
       k_runs_emit<kSrcDelta><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, ts, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+          G, M, tiles_x, td, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
       break;
     case kSrcIndex:
       k_runs_emit<kSrcIndex><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, ts, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+          G, M, tiles_x, td, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
       break;
     default:
       k_runs_emit<kSrcTrace><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, ts, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+          G, M, tiles_x, td, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
   }
 }
 
@@ -677,18 +681,19 @@ static void runs_fill(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts,
                       uint32_t* tcode, cudaStream_t st) {
   const int64_t R = (int64_t)G.P * G.C;
   const int blocks = blocks_for(R, kTraceBlock);
+  const TileDiv td = make_tile_div(ts);
   switch (seg_source(M)) {
     case kSrcDelta:
       k_runs_fill<L16, kSrcDelta><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, ts, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
+          G, M, tiles_x, td, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
       break;
     case kSrcIndex:
       k_runs_fill<L16, kSrcIndex><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, ts, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
+          G, M, tiles_x, td, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
       break;
     default:
       k_runs_fill<L16, kSrcTrace><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, ts, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
+          G, M, tiles_x, td, ray_run_off, run_slot, gseg_off, gcode_off, tlen, tcode);
   }
 }
 
@@ -722,8 +727,8 @@ void fwd_finish_k(const IterArgs& A, const TileMatrixDev& T, const float* part,
   const int b = blocks_for(R, 256);
 #define TG_FINISH(FH, CP)                                                     \
   k_fwd_finish<K, FH, CP><<<b, 256, 0, st>>>(R, T.rnrun, T.pbase, A.M.ra2, part, sino, \
-                                             out, out_mode)
-  const bool fh = A.half_factors && out_mode == FWD_RATIO;
+                                             out, out_mode, factor_offset(A.half_factors))
+  const bool fh = A.half_factors != FACT_F32 && out_mode == FWD_RATIO;
   constexpr bool kComp = K <= 8;
   if (kComp && A.comp) {
     if (fh) TG_FINISH(true, kComp); else TG_FINISH(false, kComp);

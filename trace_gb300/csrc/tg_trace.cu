@@ -17,20 +17,23 @@ constexpr int kTraceBlock = 128;
 
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_count(DevGeom G, int ngroups, int* nseg, int* rcap,
-                  unsigned* maxlen_bits, int tiles_x, int ts, int* ray_nruns) {
+                  unsigned* maxlen_bits, int tiles_x, TileDiv td, int* ray_nruns) {
   const int grp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (grp >= ngroups) return;  // warp-uniform
   const int a = grp / G.gpa;
   const int c = (grp - a * G.gpa) * 32 + lane;
   int n = 0;
-  float ml = 0.f;
+  // the longest segment: the square root is monotone and correctly rounded,
+  // so the root of the largest squared length is the largest length (one
+  // root per ray instead of one per segment)
+  float ml2 = 0.f;
   if (c < G.C) {
     if (ray_nruns) {
       int runs = 0, cur = -1, px = 0, py = 0;
-      n = trace_ray(G, a, c, [&](int, float l, float, int ix, int iy) {
-        ml = fmaxf(ml, l);
-        const int t = tile_of_pixel(ix, iy, tiles_x, ts);
+      n = trace_ray(G, a, c, [&](int, float, float l2, int ix, int iy) {
+        ml2 = fmaxf(ml2, l2);
+        const int t = tile_of_pixel(ix, iy, tiles_x, td);
         if (t != cur || !unit_step(ix, iy, px, py)) {
           ++runs;
           cur = t;
@@ -40,19 +43,21 @@ __global__ void __launch_bounds__(kTraceBlock)
       });
       ray_nruns[(int64_t)a * G.C + c] = runs;
     } else {
-      n = trace_ray(G, a, c, [&](int, float l, float, int, int) { ml = fmaxf(ml, l); });
+      n = trace_ray(G, a, c, [&](int, float, float l2, int, int) { ml2 = fmaxf(ml2, l2); });
     }
     nseg[(int64_t)a * G.C + c] = n;
   }
   const int cap = warp_max_i(n);
-  const float m = warp_max_f(ml);
+  const float m = fsqrt(warp_max_f(ml2));
   if (lane == 0) {
     rcap[grp] = cap;
     atomicMax(maxlen_bits, __float_as_uint(m));  // lengths are >= 0
   }
 }
 
-template <bool L16, bool DELTA>
+// F64: also the FP64 total of the squared lengths per ray (FP64 plans only:
+// GB300's double-precision rate is a small fraction of its single one).
+template <bool L16, bool DELTA, bool F64>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_fill(DevGeom G, MatrixDev M, int ngroups, int* ridx,
                  uint32_t* rcode, int* rstart, void* rlen, float* ra2,
@@ -101,7 +106,7 @@ __global__ void __launch_bounds__(kTraceBlock)
       reinterpret_cast<float*>(rlen)[e] = l;
     }
     a2 = fadd(a2, l2);
-    a2d = __dadd_rn(a2d, (double)l2);
+    if constexpr (F64) a2d = __dadd_rn(a2d, (double)l2);
     // backward matrix: slot = column offset inside the pixel's window
     const int slot = c - window_c0(coef, (float)ix, (float)iy);
     if (slot < 0 || slot > 1) {
@@ -138,7 +143,7 @@ __global__ void __launch_bounds__(kTraceBlock)
   if (store_fwd && DELTA && (s & 7) != 0 && s > 0)
     rcode[cbase + (int64_t)(s >> 3) * 32] = word;
   ra2[r] = a2;
-  if (ra2d) ra2d[r] = a2d;
+  if constexpr (F64) ra2d[r] = a2d;
   if (bad) {  // step codes that do not fit 4 bits
     atomicAdd(overflow, bad);
     // the first offending ray (lowest angle, then column) for the message
@@ -168,19 +173,7 @@ __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W, float* Wh
     cm = (tk - s) - yk;
     s = tk;
   };
-  for (int a = 0; a < G.P; ++a) {
-    const int64_t pos = dense_pair(M.ntiles, a, tile, lane) * 2;
-    float l0, l1;
-    if (L16) {
-      const uint32_t w =
-          reinterpret_cast<const uint32_t*>(M.dlen)[pos >> 1];
-      l0 = decode16((uint16_t)(w & 0xffffu), M.dlen_kind, M.inv_scale);
-      l1 = decode16((uint16_t)(w >> 16), M.dlen_kind, M.inv_scale);
-    } else {
-      const float2 v = reinterpret_cast<const float2*>(M.dlen)[pos >> 1];
-      l0 = v.x;
-      l1 = v.y;
-    }
+  auto add = [&](float l0, float l1) {
     if constexpr (HALF) {
       kahan(sumh, comph, __half2float(__float2half_rn(l0)));
       kahan(sumh, comph, __half2float(__float2half_rn(l1)));
@@ -190,6 +183,28 @@ __global__ void k_weights(DevGeom G, MatrixDev M, int exact, float* W, float* Wh
     } else {
       kahan(sum, comp, l0);
       kahan(sum, comp, l1);
+    }
+  };
+  // four angles per load (the lane's 16 or 32 contiguous bytes), in angle
+  // order; the padding angles past P are not added
+  for (int a4 = 0; a4 < G.P; a4 += 4) {
+    const int64_t pos = dense_pair(M.ntiles, a4, tile, lane);  // pair index
+    const int na = min(4, G.P - a4);
+    if (L16) {
+      const uint4 q = reinterpret_cast<const uint4*>(M.dlen)[pos >> 2];
+      const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (j < na)
+          add(decode16((uint16_t)(w[j] & 0xffffu), M.dlen_kind, M.inv_scale),
+              decode16((uint16_t)(w[j] >> 16), M.dlen_kind, M.inv_scale));
+    } else {
+      const float4* v = reinterpret_cast<const float4*>(M.dlen) + (pos >> 1);
+      const float4 u0 = v[0], u1 = v[1];
+      if (na > 0) add(u0.x, u0.y);
+      if (na > 1) add(u0.z, u0.w);
+      if (na > 2) add(u1.x, u1.y);
+      if (na > 3) add(u1.z, u1.w);
     }
   }
   for_each_exception(M, tile, lane, [&](float l, int, int) {
@@ -226,8 +241,8 @@ void launch_trace_count(const DevGeom& G, int* nseg, int* rcap,
                         cudaStream_t st) {
   const int ngroups = G.P * G.gpa;
   const int blocks = (ngroups * 32 + kTraceBlock - 1) / kTraceBlock;
-  k_trace_count<<<blocks, kTraceBlock, 0, st>>>(G, ngroups, nseg, rcap,
-                                                 maxlen_bits, tiles_x, ts, ray_nruns);
+  k_trace_count<<<blocks, kTraceBlock, 0, st>>>(G, ngroups, nseg, rcap, maxlen_bits,
+                                                 tiles_x, make_tile_div(ts), ray_nruns);
 }
 
 void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
@@ -238,22 +253,22 @@ void launch_trace_fill(const DevGeom& G, const MatrixDev& M, int* ridx,
   const int blocks = (ngroups * 32 + kTraceBlock - 1) / kTraceBlock;
   const bool l16 = M.len_kind != LK_F32;
   const bool delta = rcode != nullptr;
-  if (l16 && delta)
-    k_trace_fill<true, true><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow, exc,
-        exc_tile, exc_cap);
-  else if (l16)
-    k_trace_fill<true, false><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow, exc,
-        exc_tile, exc_cap);
-  else if (delta)
-    k_trace_fill<false, true><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow, exc,
-        exc_tile, exc_cap);
-  else
-    k_trace_fill<false, false><<<blocks, kTraceBlock, 0, st>>>(
-        G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow, exc,
-        exc_tile, exc_cap);
+#define TG_FILL(L, D, F)                                                          \
+  k_trace_fill<L, D, F><<<blocks, kTraceBlock, 0, st>>>(                          \
+      G, M, ngroups, ridx, rcode, rstart, rlen, ra2, ra2d, dlen, overflow, exc,   \
+      exc_tile, exc_cap)
+  if (ra2d) {  // FP64 plans (f32 lengths and explicit indices, checked at creation)
+    TG_FILL(false, false, true);
+  } else if (l16 && delta) {
+    TG_FILL(true, true, false);
+  } else if (l16) {
+    TG_FILL(true, false, false);
+  } else if (delta) {
+    TG_FILL(false, true, false);
+  } else {
+    TG_FILL(false, false, false);
+  }
+#undef TG_FILL
 }
 
 void launch_weights(const DevGeom& G, const MatrixDev& M, int exact, float* W,
