@@ -89,6 +89,36 @@ def test_half_gathers_against_fp64(alg, K, S):
     assert errs[True] < 1e-4, errs
 
 
+@pytest.mark.parametrize("alg", ["mlem", "pml"])
+def test_first_iteration_half_factors(alg):
+    """The first iteration after a reset stores halves of the factors
+    themselves (factors lie anywhere in (0, max) there), later iterations
+    halves of factor - 1: each of the first two iterations stays within
+    1e-4 relative L2 of the FP64 oracle, and a reset starts the sequence
+    again with the same bits."""
+    C, P, S = 96, 72, 8
+    th = theta_uniform(P)
+    tabs = O.angle_table(th)
+    from trace_gb300.phantom import ellipse_phantoms
+    sino = O.forward(ellipse_phantoms(C, S, seed=9, texture_sigma=0.02), tabs)
+    kw = dict(beta=0.05) if alg == "pml" else {}
+    prm = tg.default_params(alg, beta=0.05)
+    plan = tg.Plan(P, S, C, th, slices_per_pass=8, mode="fast", len_storage="u16",
+                   delta_index=True, forward_tiles=True, half_gathers=True)
+    plan.set_sinogram(sino, apply_abs=True)
+    plan.reset_recon(alg)
+    got = []
+    for it in (1, 2):
+        ref = O.run(alg, sino, tables=tabs, n_iter=it, precision=O.F64, **kw)["recon"]
+        plan.iterate(alg, 1, prm)
+        got.append(plan.get_recon(alg))
+        assert rel_l2(got[-1], ref) < 1e-4, (alg, it)
+    plan.reset_recon(alg)
+    plan.iterate(alg, 1, prm)
+    assert np.array_equal(bits(plan.get_recon(alg)), bits(got[0]))
+    plan.close()
+
+
 def test_half_gathers_keep_operator_path_fp32():
     """tg_reduce (the reference's RunParallelReduction) runs the tile-ordered
     forward with FP32 factors on a half_gathers plan (half tile, f16 lengths

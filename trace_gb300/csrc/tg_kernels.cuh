@@ -288,8 +288,10 @@ struct RunKey {
 // the ray-ordered forward matrix M when it is stored (M.rlen), else trace them.
 void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts, RunKey rk,
                       const int64_t* ray_run_off, unsigned long long* key, int* val,
-                      uint16_t* run_lp, uint16_t* run_len, int* tile_count,
-                      cudaStream_t st);
+                      uint16_t* run_lp, uint16_t* run_len, cudaStream_t st);
+// tile_first[t] = first sorted run of tile t, tile_first[ntiles] = nruns
+void launch_tile_bounds(RunKey rk, const unsigned long long* skey, int64_t nruns,
+                        int ntiles, int* tile_first, cudaStream_t st);
 int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
               int* val_in, int* val_out, int64_t n, int end_bit,
               cudaStream_t st);

@@ -370,31 +370,29 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
   if (NR > 0x7fffffff) return release(), fail(p, TG_E_GEOMETRY, "too many tile runs");
   int64_t* d_run_off;
   unsigned long long *key, *key2;
-  int *val, *val2, *tile_count, *run_slot;
+  int *val, *val2, *run_slot, *d_tile_first;
   uint16_t *run_lp, *run_len;
   if ((rc = talloc(&d_run_off, (size_t)p->R, false)) || (rc = talloc(&key, (size_t)NR, false)) ||
       (rc = talloc(&key2, (size_t)NR, false)) || (rc = talloc(&val, (size_t)NR, false)) ||
       (rc = talloc(&val2, (size_t)NR, false)) || (rc = talloc(&run_lp, (size_t)NR, false)) ||
       (rc = talloc(&run_len, (size_t)NR, false)) || (rc = talloc(&run_slot, (size_t)NR, false)) ||
-      (rc = talloc(&tile_count, (size_t)ntiles, true)))
+      (rc = talloc(&d_tile_first, (size_t)ntiles + 1, false)))
     return release(), rc;
   cudaMemcpyAsync(d_run_off, run_off.data(), p->R * 8, cudaMemcpyHostToDevice, p->st);
-  launch_runs_emit(G, p->M, tiles_x, p->fts, rk, d_run_off, key, val, run_lp, run_len, tile_count,
-                   p->st);
+  launch_runs_emit(G, p->M, tiles_x, p->fts, rk, d_run_off, key, val, run_lp, run_len, p->st);
   if (sort_runs(key, key2, val, val2, NR, end_bit, p->st))
     return release(), fail(p, TG_E_CUDA, "sorting the tile runs failed");
-  std::vector<int> tcount(ntiles);
-  cudaMemcpyAsync(tcount.data(), tile_count, ntiles * 4, cudaMemcpyDeviceToHost, p->st);
-  if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run emit failed");
+  // each tile's first run in the sorted order, from the sorted keys
+  launch_tile_bounds(rk, key2, NR, ntiles, d_tile_first, p->st);
   std::vector<int> tile_first(ntiles + 1), group_first(ntiles + 1);
-  int runs = 0, groups = 0;
+  cudaMemcpyAsync(tile_first.data(), d_tile_first, (ntiles + 1) * 4, cudaMemcpyDeviceToHost,
+                  p->st);
+  if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run emit failed");
+  int groups = 0;
   for (int t = 0; t < ntiles; ++t) {
-    tile_first[t] = runs;
     group_first[t] = groups;
-    runs += tcount[t];
-    groups += (tcount[t] + 31) / 32;
+    groups += (tile_first[t + 1] - tile_first[t] + 31) / 32;
   }
-  tile_first[ntiles] = runs;
   group_first[ntiles] = groups;
   // partial-sum slots: per group of 32 rays, one row of 32 slots per run
   // ordinal up to the group's longest run count
@@ -410,10 +408,9 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
     if (nslots > 0x7fffffff)
       return release(), fail(p, TG_E_GEOMETRY, "too many partial-sum slots");
   }
-  int *d_tile_first, *d_group_first, *gpart, *gsteps, *rnrun, *pbase;
+  int *d_group_first, *gpart, *gsteps, *rnrun, *pbase;
   uint16_t *glp, *glen;
-  if ((rc = talloc(&d_tile_first, (size_t)ntiles + 1, false)) ||
-      (rc = dalloc(p, &d_group_first, (size_t)ntiles + 1)) ||
+  if ((rc = dalloc(p, &d_group_first, (size_t)ntiles + 1)) ||
       (rc = dalloc(p, &gpart, (size_t)groups * 32)) ||
       (rc = dalloc(p, &rnrun, (size_t)p->R)) ||
       (rc = dalloc(p, &pbase, (size_t)rgroups)) ||
@@ -422,7 +419,6 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
       (rc = dalloc(p, &gsteps, (size_t)groups, true)))
     return release(), rc;
   cudaMemsetAsync(gpart, 0xff, (size_t)groups * 32 * 4, p->st);  // empty lanes: -1
-  cudaMemcpyAsync(d_tile_first, tile_first.data(), (ntiles + 1) * 4, cudaMemcpyHostToDevice, p->st);
   cudaMemcpyAsync(d_group_first, group_first.data(), (ntiles + 1) * 4, cudaMemcpyHostToDevice, p->st);
   cudaMemcpyAsync(rnrun, nruns.data(), p->R * 4, cudaMemcpyHostToDevice, p->st);
   cudaMemcpyAsync(pbase, pbase_h.data(), rgroups * 4, cudaMemcpyHostToDevice, p->st);

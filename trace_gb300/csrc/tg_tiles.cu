@@ -57,16 +57,19 @@ __device__ __forceinline__ int tile_of(int ix, int iy, int tiles_x, TileDiv d) {
 // (delta-coded or explicit indices; the stored code is the one encode16 gives
 // the traced length, so both sources yield the same tile stream), traced
 // again otherwise (forward traced on the fly, or a stray step the 4-bit code
-// cannot hold).
+// cannot hold). LEN: which length the caller takes - none (0 and 0 are
+// passed; the matrix's lengths are not read), the 16-bit code (the plan's
+// 16-bit storage) or the float length (f32 storage).
 enum SegSource { kSrcTrace = 0, kSrcDelta = 1, kSrcIndex = 2 };
+enum SegLen { kLenNone = 0, kLenCode = 1, kLenFloat = 2 };
 
-template <int SRC, bool L16, class F>
+template <int SRC, int LEN, class F>
 __device__ __forceinline__ void ray_segments(const DevGeom& G, const MatrixDev& M,
                                              int64_t r, F&& f) {
   const int a = (int)(r / G.C), c = (int)(r - (int64_t)a * G.C);
   if constexpr (SRC == kSrcTrace) {
     trace_ray(G, a, c, [&](int idx, float l, float, int ix, int iy) {
-      f(idx, ix, iy, l, L16 ? encode16(l, M.len_kind, M.scale) : (uint16_t)0);
+      f(idx, ix, iy, l, LEN == kLenCode ? encode16(l, M.len_kind, M.scale) : (uint16_t)0);
     });
   } else {
     const int g = G.C;
@@ -78,26 +81,67 @@ __device__ __forceinline__ void ray_segments(const DevGeom& G, const MatrixDev& 
     int idx = (SRC == kSrcDelta && n > 0) ? M.rstart[r] : 0;
     int ix = 0, iy = 0;
     if (SRC == kSrcDelta && n > 0) cell_xy(idx, g, inv_g, ix, iy);
-    uint32_t word = 0;
-    for (int s = 0; s < n; ++s) {
-      const int64_t e = base + (int64_t)s * 32;
-      if constexpr (SRC == kSrcDelta) {
-        if ((s & 7) == 0) word = __ldcs(M.rcode + cbase + (int64_t)(s >> 3) * 32);
-        if (s > 0) {
-          const uint32_t code = (word >> (4 * (s & 7))) & 15u;
-          const int dx = (int)(code & 1u), dy = (int)(code >> 1) - 1;
-          ix += dx;
-          iy += dy;
-          idx += dx + dy * g;
+    if constexpr (SRC == kSrcDelta) {
+      // chunks of 8 steps (one step-code word, 8 lengths), the next chunk's
+      // loads issued before the current one is walked: the walk is a chain
+      // of dependent steps, so a load issued at its step would stall it
+      struct Chunk {
+        uint32_t word;
+        uint32_t len[LEN == kLenNone ? 1 : 8];
+      };
+      auto load = [&](int ch, Chunk& k) {
+        const int s0 = ch * 8;
+        k.word = __ldcs(M.rcode + cbase + (int64_t)ch * 32);
+        if constexpr (LEN != kLenNone) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int64_t e = base + (int64_t)(s0 + j) * 32;
+            k.len[j] = 0u;
+            if (s0 + j < n) {
+              if constexpr (LEN == kLenCode)
+                k.len[j] = __ldcs(reinterpret_cast<const uint16_t*>(M.rlen) + e);
+              else
+                k.len[j] = __float_as_uint(__ldcs(reinterpret_cast<const float*>(M.rlen) + e));
+            }
+          }
         }
-      } else {
+      };
+      Chunk cur{}, nxt{};
+      if (n > 0) load(0, cur);
+      for (int ch = 0; ch * 8 < n; ++ch) {
+        if ((ch + 1) * 8 < n) load(ch + 1, nxt);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int st = ch * 8 + j;
+          if (st >= n) break;
+          if (st > 0) {
+            const uint32_t code = (cur.word >> (4 * j)) & 15u;
+            const int dx = (int)(code & 1u), dy = (int)(code >> 1) - 1;
+            ix += dx;
+            iy += dy;
+            idx += dx + dy * g;
+          }
+          if constexpr (LEN == kLenCode)
+            f(idx, ix, iy, 0.f, (uint16_t)cur.len[j]);
+          else if constexpr (LEN == kLenFloat)
+            f(idx, ix, iy, __uint_as_float(cur.len[j]), (uint16_t)0);
+          else
+            f(idx, ix, iy, 0.f, (uint16_t)0);
+        }
+        cur = nxt;
+      }
+    } else {
+      for (int st = 0; st < n; ++st) {
+        const int64_t e = base + (int64_t)st * 32;
         idx = __ldcs(M.ridx + e);
         cell_xy(idx, g, inv_g, ix, iy);
+        if constexpr (LEN == kLenCode)
+          f(idx, ix, iy, 0.f, __ldcs(reinterpret_cast<const uint16_t*>(M.rlen) + e));
+        else if constexpr (LEN == kLenFloat)
+          f(idx, ix, iy, __ldcs(reinterpret_cast<const float*>(M.rlen) + e), (uint16_t)0);
+        else
+          f(idx, ix, iy, 0.f, (uint16_t)0);
       }
-      if constexpr (L16)
-        f(idx, ix, iy, 0.f, __ldcs(reinterpret_cast<const uint16_t*>(M.rlen) + e));
-      else
-        f(idx, ix, iy, __ldcs(reinterpret_cast<const float*>(M.rlen) + e), (uint16_t)0);
     }
   }
 }
@@ -118,18 +162,21 @@ template <int SRC>
 __global__ void __launch_bounds__(kTraceBlock)
     k_runs_emit(DevGeom G, MatrixDev M, int tiles_x, TileDiv td, RunKey rk,
                 const int64_t* ray_run_off, unsigned long long* key, int* val,
-                uint16_t* run_lp, uint16_t* run_len, int* tile_count) {
+                uint16_t* run_lp, uint16_t* run_len) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= (int64_t)G.P * G.C) return;
-  int64_t i = ray_run_off[r] - 1;
+  // the ray's first run index, read once (the stores below may alias it as
+  // far as the compiler knows, which would reload it at every run)
+  const int64_t first = ray_run_off[r];
+  int64_t i = first - 1;
   int cur = -1, k = -1, len = 0, px = 0, py = 0;
   auto close = [&]() {
-    if (i >= ray_run_off[r]) {
+    if (i >= first) {
       run_len[i] = (uint16_t)len;
       key[i] = run_key(rk, cur, len, r, k);
     }
   };
-  ray_segments<SRC, false>(G, M, r, [&](int, int ix, int iy, float, uint16_t) {
+  ray_segments<SRC, kLenNone>(G, M, r, [&](int, int ix, int iy, float, uint16_t) {
     const int t = tile_of(ix, iy, tiles_x, td);
     const bool step_ok = unit_step(ix, iy, px, py);
     px = ix;
@@ -143,11 +190,22 @@ __global__ void __launch_bounds__(kTraceBlock)
       val[i] = (int)i;
       const int ts = td.ts;
       run_lp[i] = (uint16_t)((iy - tdiv(iy, td) * ts) * ts + ix - tdiv(ix, td) * ts);
-      atomicAdd(&tile_count[t], 1);
     }
     ++len;
   });
   close();
+}
+
+// First run of every tile in the sorted order (tile_first[ntiles] = nruns):
+// run j opens the tiles after the previous run's tile up to its own, the
+// last run closes the rest. Replaces per-run counters during emission.
+__global__ void k_tile_bounds(RunKey rk, const unsigned long long* skey, int64_t nruns,
+                              int ntiles, int* tile_first) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > nruns) return;
+  const int t = j < nruns ? (int)(skey[j] >> rk.tile_shift()) : ntiles;
+  const int prev = j > 0 ? (int)(skey[j - 1] >> rk.tile_shift()) : -1;
+  for (int u = prev + 1; u <= t; ++u) tile_first[u] = (int)j;
 }
 
 // One thread per run, in the sorted order of its tile: rank r in the tile is
@@ -185,7 +243,8 @@ __global__ void __launch_bounds__(kTraceBlock)
                 const int64_t* gcode_off, void* tlen, uint32_t* tcode) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= (int64_t)G.P * G.C) return;
-  int64_t i = ray_run_off[r] - 1;
+  const int64_t first = ray_run_off[r];  // read once, as in k_runs_emit
+  int64_t i = first - 1;
   int cur = -1, s = 0, px = 0, py = 0;
   int64_t lbase = 0, cbase = 0;
   uint32_t w0 = 0, w1 = 0;  // the chunk's step bytes (steps 0-3, 4-7)
@@ -218,12 +277,13 @@ __global__ void __launch_bounds__(kTraceBlock)
     *reinterpret_cast<uint2*>(tcode + cbase + (int64_t)c * 64) = make_uint2(w0, w1);
   };
   auto flush = [&]() {  // a run's last, partial chunk: zero lengths after it
-    if (i >= ray_run_off[r] && (s & 7) != 0) {
+    if (i >= first && (s & 7) != 0) {
       for (int k = s & 7; k < 8; ++k) push(0u);
       store(s >> 3);
     }
   };
-  ray_segments<SRC, L16>(G, M, r, [&](int, int ix, int iy, float l, uint16_t code) {
+  ray_segments<SRC, L16 ? kLenCode : kLenFloat>(
+      G, M, r, [&](int, int ix, int iy, float l, uint16_t code) {
     const int t = tile_of(ix, iy, tiles_x, td);
     if (t != cur || !unit_step(ix, iy, px, py)) {
       flush();
@@ -627,23 +687,22 @@ static int seg_source(const MatrixDev& M) {
 
 void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts, RunKey rk,
                       const int64_t* ray_run_off, unsigned long long* key, int* val,
-                      uint16_t* run_lp, uint16_t* run_len, int* tile_count,
-                      cudaStream_t st) {
+                      uint16_t* run_lp, uint16_t* run_len, cudaStream_t st) {
   const int64_t R = (int64_t)G.P * G.C;
   const int blocks = blocks_for(R, kTraceBlock);
   const TileDiv td = make_tile_div(ts);
   switch (seg_source(M)) {
     case kSrcDelta:
       k_runs_emit<kSrcDelta><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, td, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+          G, M, tiles_x, td, rk, ray_run_off, key, val, run_lp, run_len);
       break;
     case kSrcIndex:
       k_runs_emit<kSrcIndex><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, td, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+          G, M, tiles_x, td, rk, ray_run_off, key, val, run_lp, run_len);
       break;
     default:
       k_runs_emit<kSrcTrace><<<blocks, kTraceBlock, 0, st>>>(
-          G, M, tiles_x, td, rk, ray_run_off, key, val, run_lp, run_len, tile_count);
+          G, M, tiles_x, td, rk, ray_run_off, key, val, run_lp, run_len);
   }
 }
 
@@ -661,6 +720,12 @@ int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
   cudaStreamSynchronize(st);
   cudaFree(tmp);
   return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+void launch_tile_bounds(RunKey rk, const unsigned long long* skey, int64_t nruns,
+                        int ntiles, int* tile_first, cudaStream_t st) {
+  k_tile_bounds<<<blocks_for(nruns + 1, 256), 256, 0, st>>>(rk, skey, nruns, ntiles,
+                                                            tile_first);
 }
 
 void launch_runs_group(RunKey rk, const unsigned long long* skey, const int* sval,
