@@ -46,9 +46,10 @@
  * cudaMallocHost, or cudaHostRegister'ed and mapped) is read or written in
  * place by the kernels that convert between the reference layout and the
  * device layout, across the CPU-GPU link, with no device staging copy; a
- * pageable buffer goes through a device staging buffer. Either way a call
- * that takes a host buffer returns after it has read (uploads) or written
- * (downloads) it.
+ * pageable buffer, and a download into memory registered read-only
+ * (cudaHostRegisterReadOnly), go through a device staging buffer. Either
+ * way a call that takes a host buffer returns after it has read (uploads)
+ * or written (downloads) it.
  */
 #ifndef TRACE_GB300_H
 #define TRACE_GB300_H

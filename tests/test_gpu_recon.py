@@ -276,6 +276,13 @@ def test_page_locked_transfers_match_staged():
         return plan
 
     plans = {k: run(k) for k in ("pageable", "locked", "device")}
+    # the page-locked plan has staged nothing (no staging buffer allocated),
+    # also after a download into page-locked memory; the pageable one has
+    held = plans["locked"].info()["device_bytes"]
+    out0 = torch.empty(plans["pageable"].get_recon(alg).shape, dtype=torch.float32).pin_memory()
+    plans["locked"].get_recon(alg, out=out0)
+    assert plans["locked"].info()["device_bytes"] == held
+    assert plans["pageable"].info()["device_bytes"] > held
     want = plans["pageable"].get_recon(alg)
     for k, plan in plans.items():
         assert np.array_equal(bits(plan.get_recon(alg)), bits(want)), k

@@ -1,6 +1,8 @@
 // Host side of the C ABI declared in include/trace_gb300.h: plan creation
 // (geometry tables, tracing, matrix construction), state upload/download,
 // and the per-iteration launch sequence.
+#include <cuda.h>
+
 #include <algorithm>
 #include <map>
 #include <cmath>
@@ -193,6 +195,42 @@ float* mapped_host(const void* ptr, size_t n) {
       last - first)
     return nullptr;
   return static_cast<float*>(a.devicePointer);
+}
+
+// Whether kernels may write the host memory at `ptr` (for downloads into a
+// mapped buffer): memory registered read-only (cudaHostRegisterReadOnly) is
+// mapped for device reads only, and writing it from a kernel would be an
+// invalid access, so such a buffer takes the staged copy instead. The
+// driver's pointer attribute is reached through the runtime's entry-point
+// query (no link against the driver library); if it cannot be asked, the
+// answer is no.
+bool device_writable(const void* ptr) {
+  using GetAttr = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+  static const GetAttr get = []() -> GetAttr {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    return reinterpret_cast<GetAttr>(fn);
+  }();
+  if (!get) return false;
+  unsigned int flags = 0;
+  if (get(&flags, CU_POINTER_ATTRIBUTE_ACCESS_FLAGS, (CUdeviceptr)(uintptr_t)ptr) !=
+      CUDA_SUCCESS)
+    return false;
+  return flags == CU_POINTER_ATTRIBUTE_ACCESS_FLAG_READWRITE;
+}
+
+// mapped_host for a buffer the kernels will write: both ends writable too.
+float* mapped_host_out(void* ptr, size_t n) {
+  float* m = mapped_host(ptr, n);
+  if (!m) return nullptr;
+  const char* last = static_cast<const char*>(ptr) + (n - 1) * sizeof(float);
+  return device_writable(ptr) && device_writable(last) ? m : nullptr;
 }
 
 // Stage host data through one reusable device buffer.
@@ -1059,7 +1097,7 @@ int tg_get_recon(tg_plan* p, int alg, float* recon, int on_device) {
   const int nuser = p->S + 2 * p->halo;
   const size_t n = (size_t)nuser * p->g2;
   float* dst = recon;
-  float* mapped = on_device ? nullptr : mapped_host(recon, n);
+  float* mapped = on_device ? nullptr : mapped_host_out(recon, n);
   if (!on_device) {
     if (mapped) {
       dst = mapped;
@@ -1707,7 +1745,7 @@ int tg_get_replica(tg_plan* p, int alg, float* replica, int on_device) {
   if (!p->d_rep) return fail(p, TG_E_STATE, "no replica: call tg_reduce first");
   const size_t n = (size_t)p->S * p->g2 * 2;
   float* dst = replica;
-  float* mapped = on_device ? nullptr : mapped_host(replica, n);
+  float* mapped = on_device ? nullptr : mapped_host_out(replica, n);
   if (!on_device) {
     if (mapped) {
       dst = mapped;
@@ -1789,7 +1827,7 @@ int tg_forward_project(tg_plan* p, int alg, const tg_params* prm, float* sim,
   TG_TRY(check_layout(p, alg));
   const size_t packed = (size_t)p->nb * p->R * p->K;
   const size_t n = (size_t)p->P * p->S * p->C;
-  float* mapped = on_device ? nullptr : mapped_host(sim, n);
+  float* mapped = on_device ? nullptr : mapped_host_out(sim, n);
   const bool staged = !on_device && !mapped;
   TG_TRY(stage(p, packed + (staged ? n : 0)));
   const IterArgs A = make_args(p, alg, prm);
