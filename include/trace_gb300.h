@@ -237,6 +237,15 @@ int tg_plan_get_timing(tg_plan* plan, tg_timing* out);
 /* In-place degrees -> radians with the reference's float constant. Host. */
 int tg_degree_to_radian(float* theta, int n);
 
+/* Page-locked host memory for sinograms and reconstructions (so that the
+ * transfers read and write it in place; see the conventions above), for
+ * hosts that do not call the CUDA runtime themselves. tg_host_alloc stores
+ * the address in *out (NULL for bytes == 0) or returns TG_E_NOMEM;
+ * tg_host_free(NULL) does nothing. No plan is involved: tg_last_error(NULL)
+ * holds the message of a failure. */
+int tg_host_alloc(size_t bytes, void** out);
+int tg_host_free(void* ptr);
+
 /* Sinogram in the reference layout [P][S][C] float32. `on_device` != 0 means
  * `sino` is a device pointer. apply_abs != 0 applies |x| (trace_utils::Absolute)
  * during the upload. */

@@ -97,6 +97,29 @@ def test_driver_builds_and_rejects_bad_usage(lib):
     assert r.returncode == 1 and "cannot open" in r.stderr
 
 
+def test_driver_checks_npy_inputs(lib, tmp_path):
+    """The driver's .npy reader (format 1-3, little-endian float32, C
+    order) rejects other dtypes, ranks and shapes before any device work."""
+    import subprocess
+    drv = tgb.build_driver()
+    th = tmp_path / "t.npy"
+    np.save(th, np.zeros(4, np.float32))
+    cases = [(np.zeros((4, 1, 8), np.float64), [], "float32"),
+             (np.zeros((4, 8), np.float32), [], "3-dimensional"),
+             (np.zeros((4, 1, 8), np.float32), ["-P", "5"], "does not match"),
+             (np.asfortranarray(np.zeros((4, 2, 8), np.float32)), [], "C order")]
+    for i, (arr, extra, msg) in enumerate(cases):
+        sf = tmp_path / f"s{i}.npy"
+        np.save(sf, arr)
+        r = subprocess.run([drv, "-r", "sirt", "-f", str(sf), "-t", str(th),
+                            "-o", str(tmp_path / "r.npy"), *extra],
+                           capture_output=True, text=True)
+        assert r.returncode == 1 and msg in r.stderr, (msg, r.stderr)
+    r = subprocess.run([drv, "-r", "sirt", "-f", str(tmp_path / "s.f32"), "-t", str(th),
+                        "-o", str(tmp_path / "r.npy")], capture_output=True, text=True)
+    assert r.returncode == 1
+
+
 def test_ctypes_structures_match_the_header(tmp_path):
     """The Python binding's ctypes structures have the C header's layout:
     size and every field's offset, as a C compiler lays them out."""

@@ -7,6 +7,7 @@ import subprocess
 import numpy as np
 import pytest
 
+import trace_gb300 as tg
 from oracle import oracle as O
 from tests._util import rel_l2, theta_uniform
 from trace_gb300 import build as tgb
@@ -49,3 +50,30 @@ def test_driver_matches_oracle(tmp_path, alg, extra, params):
     want = O.run(alg, sino, theta=th, n_iter=n, **params)["recon"]
     tol = 1e-4 if "--fast" in extra else 2e-6
     assert rel_l2(got, want) < tol
+
+
+@pytest.mark.parametrize("alg", ["sirt", "apmlr"])
+def test_driver_npy_files(tmp_path, alg):
+    """NumPy files in and out: the shapes come from the sinogram, theta is
+    given in degrees (--degrees), and the result matches the oracle."""
+    tgb.build()
+    drv = tgb.build_driver()
+    C, P, S, n = 40, 36, 2, 2
+    th = theta_uniform(P)
+    deg = (th.astype(np.float64) * 180.0 / np.pi).astype(np.float32)
+    rng = np.random.default_rng(5)
+    sino = rng.uniform(0.5, 2.0, (P, S, C)).astype(np.float32)
+    np.save(tmp_path / "s.npy", sino)
+    np.save(tmp_path / "t.npy", deg)
+    r = subprocess.run([drv, "-r", alg, "-f", str(tmp_path / "s.npy"), "-t",
+                        str(tmp_path / "t.npy"), "-o", str(tmp_path / "r.npy"),
+                        "-i", str(n), "--degrees", "-j", "0.4"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = np.load(tmp_path / "r.npy")
+    halo = 1 if alg == "apmlr" else 0
+    assert got.shape == (S + 2 * halo, C, C) and got.dtype == np.float32
+    rad = tg.degree_to_radian(deg)
+    kw = {"beta": 0.4} if alg == "apmlr" else {}
+    want = O.run(alg, sino, theta=rad, n_iter=n, **kw)["recon"]
+    assert rel_l2(got, want) < 2e-6

@@ -315,6 +315,31 @@ def test_page_locked_transfers_match_staged():
         plan.close()
 
 
+def test_host_empty_buffers_are_used_in_place():
+    """tg.host_empty (tg_host_alloc) gives page-locked arrays: an upload from
+    and a download into them allocate no staging buffer, with the same bits
+    as ordinary arrays."""
+    f = golden("recon_mlem.npz")
+    alg = str(f["alg"])
+    sino = tg.host_empty(f["sino"].shape)
+    sino[...] = f["sino"]
+    outs = []
+    for src in (np.array(f["sino"], np.float32), sino):
+        plan = plan_for(f)
+        plan.set_sinogram(src, apply_abs=True)
+        plan.reset_recon(alg)
+        plan.iterate(alg, 2, params_of(f))
+        held = plan.info()["device_bytes"]
+        out = tg.host_empty((int(f["S"]), int(f["C"]), int(f["C"])))
+        plan.get_recon(alg, out=out)
+        if src is sino:
+            assert plan.info()["device_bytes"] == held
+        outs.append(np.array(out))
+        plan.close()
+    assert np.array_equal(bits(outs[0]), bits(outs[1]))
+    del sino, out  # freed with the arrays (tg_host_free)
+
+
 @pytest.mark.parametrize("P", [1920, 1921, 2003])
 def test_many_angles(P):
     """Angle counts past several 512-angle chunks of the backprojection's

@@ -37,7 +37,7 @@ EXPORTED = [
     "tg_forward_project", "tg_trace_rays", "tg_plan_set_timing",
     "tg_plan_get_timing", "tg_plan_set_graphs", "tg_batch_create",
     "tg_batch_iterate", "tg_batch_synchronize", "tg_batch_destroy",
-    "tg_batch_last_error", "tg_batch_get_info",
+    "tg_batch_last_error", "tg_batch_get_info", "tg_host_alloc", "tg_host_free",
 ]
 
 
@@ -100,6 +100,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.tg_plan_create.argtypes = [C.POINTER(PlanDesc), vp, vp, vp, C.POINTER(vp)]
     lib.tg_batch_last_error.restype = C.c_char_p
     lib.tg_batch_last_error.argtypes = [vp]
+    lib.tg_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
+    lib.tg_host_free.argtypes = [vp]
     for name in EXPORTED:
         getattr(lib, name)  # every declared symbol must exist
     _lib = lib
@@ -131,6 +133,37 @@ def _host_out(out, shape):
             or view.shape != tuple(shape) or not view.flags.c_contiguous):
         raise ValueError(f"out must be a C-contiguous float32 array of shape {tuple(shape)}")
     return out
+
+
+class _HostBlock:
+    """Page-locked host memory from tg_host_alloc, freed with the object."""
+
+    def __init__(self, nbytes):
+        self._lib = load_library()
+        self.ptr = C.c_void_p()
+        rc = self._lib.tg_host_alloc(C.c_size_t(nbytes), C.byref(self.ptr))
+        if rc:
+            raise TraceError(rc, self._lib.tg_last_error(None).decode())
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and self.ptr.value:
+            self._lib.tg_host_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+
+def host_empty(shape, dtype=np.float32) -> np.ndarray:
+    """An uninitialised C-contiguous host array in page-locked memory
+    (tg_host_alloc): sinograms uploaded from it and reconstructions, replicas
+    and projections downloaded into it are read and written in place by the
+    plan's kernels. The memory is freed when the array is."""
+    shape = tuple(int(s) for s in np.atleast_1d(shape))
+    n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+    if n == 0:
+        return np.empty(shape, dtype)
+    block = _HostBlock(n)
+    raw = (C.c_char * n).from_address(block.ptr.value)
+    raw._block = block  # the array keeps raw alive, raw keeps the block
+    return np.frombuffer(raw, dtype=dtype).reshape(shape)
 
 
 def default_params(alg: str, beta=None, beta1=1.0, delta=1.0, delta1=1.0,

@@ -555,6 +555,31 @@ int tg_degree_to_radian(float* theta, int n) {
   return TG_OK;
 }
 
+int tg_host_alloc(size_t bytes, void** out) {
+  if (!out) return fail(nullptr, TG_E_ARG, "null output");
+  *out = nullptr;
+  if (bytes == 0) return TG_OK;
+  const cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return fail(nullptr, TG_E_NOMEM, "cudaHostAlloc of " + std::to_string(bytes) +
+                                         " bytes failed: " + cudaGetErrorString(e));
+  }
+  return TG_OK;
+}
+
+int tg_host_free(void* ptr) {
+  if (!ptr) return TG_OK;
+  const cudaError_t e = cudaFreeHost(ptr);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(nullptr, TG_E_CUDA, std::string("cudaFreeHost failed: ") +
+                                        cudaGetErrorString(e));
+  }
+  return TG_OK;
+}
+
 int tg_plan_create(const tg_plan_desc* desc, const float* theta,
                    const float* sin_tab, const float* cos_tab, tg_plan** out) {
   if (!desc || !theta || !out) return fail(nullptr, TG_E_ARG, "null argument");

@@ -49,7 +49,7 @@ struct Options {
   int forward_on_the_fly = 0;  // trace rays during the forward projection
   int compensated = 0;      // fast mode + forward_tiles: Kahan ray/pixel sums
   int backward_tile_width = 0;  // 8 (default), 16 or 4 pixels per tile row
-  int forward_tile_side = 0;    // 64 (default), 32 or 96
+  int forward_tile_side = 0;    // 64 (default); 32 to 96 in steps of 16
   int batch_streams = 0;        // 2 (default): odd slice batches on a 2nd stream
   int forward_block_warps = 0;  // 32 (default), 16 or 8 warps per forward tile
 };
@@ -114,10 +114,17 @@ class GpuTraceMetadata {
 
   // The reconstruction, (num_slices + 2*halo) x grid x grid, on the host.
   std::vector<float> recon(int alg) const {
-    std::vector<float> out((size_t)(num_slices_ + 2 * halo_) * num_grids_ *
-                           num_grids_);
+    std::vector<float> out(recon_count());
     check(tg_get_recon(plan_.get(), alg, out.data(), 0), plan_.get());
     return out;
+  }
+  // Into a caller's host buffer of recon_count() floats (page-locked memory,
+  // e.g. from tg_host_alloc, is written in place).
+  void recon_into(int alg, float* out) const {
+    check(tg_get_recon(plan_.get(), alg, out, 0), plan_.get());
+  }
+  size_t recon_count() const {
+    return (size_t)(num_slices_ + 2 * halo_) * num_grids_ * num_grids_;
   }
 
  private:
