@@ -289,6 +289,21 @@ struct RunKey {
 void launch_runs_emit(const DevGeom& G, const MatrixDev& M, int tiles_x, int ts, RunKey rk,
                       const int64_t* ray_run_off, unsigned long long* key, int* val,
                       uint16_t* run_lp, uint16_t* run_len, cudaStream_t st);
+// Construction prefix sums (tg_tiles.cu): tmp == nullptr asks for the
+// temporary bytes; counts (int) to int64 offsets, or int64 to int64.
+cudaError_t scan_counts(void* tmp, size_t* tmp_bytes, const int* in, int64_t* out, int n,
+                        cudaStream_t st);
+cudaError_t scan_i64(void* tmp, size_t* tmp_bytes, const int64_t* in, int64_t* out, int n,
+                     cudaStream_t st);
+// gslots[g] = 32 x the longest run count of ray group g (32 rays)
+void launch_group_slots(const int* nruns, int64_t R, int64_t* gslots, cudaStream_t st);
+// out[g] = tile-stream entries of run group g (256 per 8-step chunk)
+void launch_group_entries(const int* gsteps, int groups, int64_t* out, cudaStream_t st);
+// out[i] = in[i] >> shift (as int, or int64)
+void launch_shift_narrow_i32(const int64_t* in, int* out, int64_t n, int shift,
+                             cudaStream_t st);
+void launch_shift_i64(const int64_t* in, int64_t* out, int64_t n, int shift,
+                      cudaStream_t st);
 // tile_first[t] = first sorted run of tile t, tile_first[ntiles] = nruns
 void launch_tile_bounds(RunKey rk, const unsigned long long* skey, int64_t nruns,
                         int ntiles, int* tile_first, cudaStream_t st);

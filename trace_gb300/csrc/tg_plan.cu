@@ -376,7 +376,7 @@ float* batch_ptr(tg_plan* p, float* base, int batch_slot) {
 
 // Tile-ordered forward matrix (tg_tiles.cu): runs of each ray inside 64x64
 // tiles, sorted by (tile, chunk-count class, ray) and packed 32 per warp group.
-int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
+int build_tiles(tg_plan* p, int* d_nruns) {
   const DevGeom& G = p->G;
   const int C = p->C;
   const int tiles_x = (C + p->fts - 1) / p->fts;
@@ -399,24 +399,59 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
     tmp.clear();
   };
   int rc = TG_OK;
-  std::vector<int64_t> run_off(p->R);
-  int64_t NR = 0;
-  for (int64_t r = 0; r < p->R; ++r) {
-    run_off[r] = NR;
-    NR += nruns[r];
+  // Offsets on the device (prefix sums, no round trip through the host):
+  // each ray's first run, each 32-ray group's first partial-sum slot (32
+  // per run ordinal up to the group's longest run count); only the totals
+  // come back, to size the buffers.
+  const int64_t rgroups = (p->R + 31) / 32;
+  int64_t *d_run_off, *d_gslots, *d_pbase64;
+  if ((rc = talloc(&d_run_off, (size_t)p->R, false)) ||
+      (rc = talloc(&d_gslots, (size_t)rgroups, false)) ||
+      (rc = talloc(&d_pbase64, (size_t)rgroups, false)))
+    return release(), rc;
+  char* scan_tmp = nullptr;
+  size_t scan_bytes = 0;
+  // temporary storage for one prefix sum (CUB), grown as needed
+  auto scan_space = [&](size_t need) -> int {
+    if (need <= scan_bytes) return TG_OK;
+    int r2 = talloc(&scan_tmp, need, false);
+    if (r2 == TG_OK) scan_bytes = need;
+    return r2;
+  };
+  {
+    size_t b1 = 0, b2 = 0;
+    if (scan_counts(nullptr, &b1, d_nruns, d_run_off, (int)p->R, p->st) != cudaSuccess ||
+        scan_i64(nullptr, &b2, d_gslots, d_pbase64, (int)rgroups, p->st) != cudaSuccess)
+      return release(), fail(p, TG_E_CUDA, "prefix-sum setup failed");
+    if ((rc = scan_space(std::max(b1, b2)))) return release(), rc;
+    b1 = b2 = scan_bytes;
+    launch_group_slots(d_nruns, p->R, d_gslots, p->st);
+    if (scan_counts(scan_tmp, &b1, d_nruns, d_run_off, (int)p->R, p->st) != cudaSuccess ||
+        scan_i64(scan_tmp, &b2, d_gslots, d_pbase64, (int)rgroups, p->st) != cudaSuccess)
+      return release(), fail(p, TG_E_CUDA, "prefix sums failed");
   }
+  int64_t last_off = 0, last_base = 0, last_slots = 0;
+  int last_runs = 0;
+  cudaMemcpyAsync(&last_off, d_run_off + p->R - 1, 8, cudaMemcpyDeviceToHost, p->st);
+  cudaMemcpyAsync(&last_runs, d_nruns + p->R - 1, 4, cudaMemcpyDeviceToHost, p->st);
+  cudaMemcpyAsync(&last_base, d_pbase64 + rgroups - 1, 8, cudaMemcpyDeviceToHost, p->st);
+  cudaMemcpyAsync(&last_slots, d_gslots + rgroups - 1, 8, cudaMemcpyDeviceToHost, p->st);
+  if (cudaStreamSynchronize(p->st) != cudaSuccess)
+    return release(), fail(p, TG_E_CUDA, "run counting failed");
+  const int64_t NR = last_off + last_runs;
+  const int64_t nslots = last_base + last_slots;
   if (NR > 0x7fffffff) return release(), fail(p, TG_E_GEOMETRY, "too many tile runs");
-  int64_t* d_run_off;
+  if (nslots > 0x7fffffff)
+    return release(), fail(p, TG_E_GEOMETRY, "too many partial-sum slots");
   unsigned long long *key, *key2;
   int *val, *val2, *run_slot, *d_tile_first;
   uint16_t *run_lp, *run_len;
-  if ((rc = talloc(&d_run_off, (size_t)p->R, false)) || (rc = talloc(&key, (size_t)NR, false)) ||
+  if ((rc = talloc(&key, (size_t)NR, false)) ||
       (rc = talloc(&key2, (size_t)NR, false)) || (rc = talloc(&val, (size_t)NR, false)) ||
       (rc = talloc(&val2, (size_t)NR, false)) || (rc = talloc(&run_lp, (size_t)NR, false)) ||
       (rc = talloc(&run_len, (size_t)NR, false)) || (rc = talloc(&run_slot, (size_t)NR, false)) ||
       (rc = talloc(&d_tile_first, (size_t)ntiles + 1, false)))
     return release(), rc;
-  cudaMemcpyAsync(d_run_off, run_off.data(), p->R * 8, cudaMemcpyHostToDevice, p->st);
   launch_runs_emit(G, p->M, tiles_x, p->fts, rk, d_run_off, key, val, run_lp, run_len, p->st);
   if (sort_runs(key, key2, val, val2, NR, end_bit, p->st))
     return release(), fail(p, TG_E_CUDA, "sorting the tile runs failed");
@@ -432,25 +467,10 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
     groups += (tile_first[t + 1] - tile_first[t] + 31) / 32;
   }
   group_first[ntiles] = groups;
-  // partial-sum slots: per group of 32 rays, one row of 32 slots per run
-  // ordinal up to the group's longest run count
-  const int64_t rgroups = (p->R + 31) / 32;
-  std::vector<int> pbase_h(rgroups);
-  int64_t nslots = 0;
-  for (int64_t gi = 0; gi < rgroups; ++gi) {
-    int most = 0;
-    for (int64_t r = gi * 32; r < std::min<int64_t>(p->R, gi * 32 + 32); ++r)
-      most = std::max(most, nruns[r]);
-    pbase_h[gi] = (int)nslots;
-    nslots += (int64_t)most * 32;
-    if (nslots > 0x7fffffff)
-      return release(), fail(p, TG_E_GEOMETRY, "too many partial-sum slots");
-  }
-  int *d_group_first, *gpart, *gsteps, *rnrun, *pbase;
+  int *d_group_first, *gpart, *gsteps, *pbase;
   uint16_t *glp, *glen;
   if ((rc = dalloc(p, &d_group_first, (size_t)ntiles + 1)) ||
       (rc = dalloc(p, &gpart, (size_t)groups * 32)) ||
-      (rc = dalloc(p, &rnrun, (size_t)p->R)) ||
       (rc = dalloc(p, &pbase, (size_t)rgroups)) ||
       (rc = dalloc(p, &glp, (size_t)groups * 32, true)) ||
       (rc = dalloc(p, &glen, (size_t)groups * 32, true)) ||
@@ -458,29 +478,40 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
     return release(), rc;
   cudaMemsetAsync(gpart, 0xff, (size_t)groups * 32 * 4, p->st);  // empty lanes: -1
   cudaMemcpyAsync(d_group_first, group_first.data(), (ntiles + 1) * 4, cudaMemcpyHostToDevice, p->st);
-  cudaMemcpyAsync(rnrun, nruns.data(), p->R * 4, cudaMemcpyHostToDevice, p->st);
-  cudaMemcpyAsync(pbase, pbase_h.data(), rgroups * 4, cudaMemcpyHostToDevice, p->st);
+  launch_shift_narrow_i32(d_pbase64, pbase, rgroups, 0, p->st);  // checked above
   launch_runs_group(rk, key2, val2, NR, d_tile_first, d_group_first, run_lp, run_len,
                     d_run_off, pbase, gpart, glp, glen, gsteps, run_slot, p->st);
-  std::vector<int> steps(groups);
-  cudaMemcpyAsync(steps.data(), gsteps, (size_t)groups * 4, cudaMemcpyDeviceToHost, p->st);
-  if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run grouping failed");
-  std::vector<int64_t> seg_off(groups), code_off(groups);
-  int64_t entries = 0, words = 0;
-  for (int gi = 0; gi < groups; ++gi) {
-    seg_off[gi] = entries;
-    code_off[gi] = words;
-    entries += (int64_t)((steps[gi] + 7) / 8) * 256;  // chunks of 8 steps
-    words += (int64_t)((steps[gi] + 7) / 8) * 64;  // 8 step bytes per lane
+  // the groups' tile-stream offsets: 256 entries (and 64 step words) per
+  // chunk of 8 steps of the group's longest run
+  int64_t *d_seg_off, *d_code_off, *d_gentries;
+  if ((rc = dalloc(p, &d_seg_off, (size_t)groups)) ||
+      (rc = dalloc(p, &d_code_off, (size_t)groups)) ||
+      (rc = talloc(&d_gentries, (size_t)groups, false)))
+    return release(), rc;
+  int64_t entries = 0;
+  if (groups > 0) {
+    size_t b3 = 0;
+    if (scan_i64(nullptr, &b3, d_gentries, d_seg_off, groups, p->st) != cudaSuccess)
+      return release(), fail(p, TG_E_CUDA, "prefix-sum setup failed");
+    if ((rc = scan_space(b3))) return release(), rc;
+    b3 = scan_bytes;
+    launch_group_entries(gsteps, groups, d_gentries, p->st);
+    if (scan_i64(scan_tmp, &b3, d_gentries, d_seg_off, groups, p->st) != cudaSuccess)
+      return release(), fail(p, TG_E_CUDA, "prefix sums failed");
+    launch_shift_i64(d_seg_off, d_code_off, groups, 2, p->st);  // 64 words per 256 entries
+    int64_t last_seg = 0, last_entries = 0;
+    cudaMemcpyAsync(&last_seg, d_seg_off + groups - 1, 8, cudaMemcpyDeviceToHost, p->st);
+    cudaMemcpyAsync(&last_entries, d_gentries + groups - 1, 8, cudaMemcpyDeviceToHost, p->st);
+    if (cudaStreamSynchronize(p->st) != cudaSuccess)
+      return release(), fail(p, TG_E_CUDA, "run grouping failed");
+    entries = last_seg + last_entries;
   }
+  const int64_t words = entries / 4;
   const bool l16 = p->len_kind != TG_LEN_F32;
-  int64_t *d_seg_off, *d_code_off;
   uint32_t* tcode;
   void* tlen = nullptr;
   // unused steps keep the "stay" step 0 (tg_tiles.cu)
-  if ((rc = dalloc(p, &d_seg_off, (size_t)groups)) || (rc = dalloc(p, &d_code_off, (size_t)groups)) ||
-      (rc = dalloc(p, &tcode, (size_t)words, true)))
-    return release(), rc;
+  if ((rc = dalloc(p, &tcode, (size_t)words, true))) return release(), rc;
   if (l16) {
     uint16_t* t;
     if ((rc = dalloc(p, &t, (size_t)entries, true))) return release(), rc;
@@ -490,8 +521,6 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
     if ((rc = dalloc(p, &t, (size_t)entries, true))) return release(), rc;
     tlen = t;
   }
-  cudaMemcpyAsync(d_seg_off, seg_off.data(), groups * 8, cudaMemcpyHostToDevice, p->st);
-  cudaMemcpyAsync(d_code_off, code_off.data(), groups * 8, cudaMemcpyHostToDevice, p->st);
   launch_runs_fill(G, p->M, tiles_x, p->fts, d_run_off, run_slot, d_seg_off, d_code_off, tlen,
                    tcode, p->st);
   if (cudaStreamSynchronize(p->st) != cudaSuccess) return release(), fail(p, TG_E_CUDA, "run fill failed");
@@ -504,7 +533,7 @@ int build_tiles(tg_plan* p, const std::vector<int>& nruns) {
   T.bw = p->d.forward_block_warps ? p->d.forward_block_warps : 32;
   T.group_first = d_group_first;
   T.gpart = gpart;
-  T.rnrun = rnrun;
+  T.rnrun = d_nruns;
   T.pbase = pbase;
   T.glp = glp;
   T.glen = glen;
@@ -740,16 +769,14 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
       (rc = dalloc(p, &p->d_overflow, 3, true)))
     return bail(rc);
   // runs per ray of the tile-ordered forward matrix, counted in the same pass
+  // (kept on the device: the tile build's offsets and the finish kernel's
+  // per-ray run counts)
   int* d_nruns = nullptr;
-  std::vector<int> h_nruns;
   if (d.forward_tiles) {
     if ((rc = dalloc(p, &d_nruns, (size_t)p->R))) return bail(rc);
-    h_nruns.resize(p->R);
   }
   launch_trace_count(G, p->d_rnseg, p->d_rcap, p->d_maxlen, (C + p->fts - 1) / p->fts,
                      p->fts, d_nruns, p->st);
-  if (d_nruns)
-    cudaMemcpyAsync(h_nruns.data(), d_nruns, p->R * 4, cudaMemcpyDeviceToHost, p->st);
   std::vector<int> rcap(ngroups);
   unsigned maxbits = 0;
   p->h_nseg.resize(p->R);
@@ -757,7 +784,6 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   cudaMemcpyAsync(&maxbits, p->d_maxlen, 4, cudaMemcpyDeviceToHost, p->st);
   cudaMemcpyAsync(p->h_nseg.data(), p->d_rnseg, p->R * 4, cudaMemcpyDeviceToHost, p->st);
   const cudaError_t traced = cudaStreamSynchronize(p->st);
-  if (d_nruns) dfree(p, d_nruns, (size_t)p->R * sizeof(int));
   if (traced != cudaSuccess) {
     p->err = std::string("tracing failed: ") + cudaGetErrorString(cudaGetLastError());
     return bail(TG_E_CUDA);
@@ -921,7 +947,7 @@ int tg_plan_create(const tg_plan_desc* desc, const float* theta,
   if (p->fp64) launch_weights64(G, M, p->d_W64, p->st);
   p->info.window_exceptions = (int64_t)nexc;
   (void)counters[1];
-  if (d.forward_tiles && (rc = build_tiles(p, h_nruns))) {
+  if (d.forward_tiles && (rc = build_tiles(p, d_nruns))) {
     if (p->err.empty()) p->err = "building the tile-ordered forward matrix failed";
     return bail(rc);
   }

@@ -27,6 +27,8 @@
 // filled. Emission and fill walk each ray's segments in the stored
 // ray-ordered matrix, or trace the ray again when the plan keeps none.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+#include <cuda/std/functional>
 
 #include "tg_kernels.cuh"
 
@@ -194,6 +196,30 @@ __global__ void __launch_bounds__(kTraceBlock)
     ++len;
   });
   close();
+}
+
+// Per group of 32 rays: its partial-sum slots, 32 per run ordinal up to the
+// group's longest run count.
+__global__ void k_group_slots(const int* __restrict__ nruns, int64_t R, int64_t* gslots) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g * 32 >= R) return;
+  int most = 0;
+  const int64_t end = min(R, g * 32 + 32);
+  for (int64_t r = g * 32; r < end; ++r) most = max(most, nruns[r]);
+  gslots[g] = (int64_t)most * 32;
+}
+
+// Per run group: its tile-stream entries, 256 per chunk of 8 steps.
+__global__ void k_group_entries(const int* __restrict__ gsteps, int groups, int64_t* out) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < groups) out[g] = (int64_t)((gsteps[g] + 7) / 8) * 256;
+}
+
+// out[i] = in[i] >> shift, narrowed to T (values checked on the host first).
+template <class T>
+__global__ void k_shift_narrow(const int64_t* __restrict__ in, T* out, int64_t n, int shift) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (T)(in[i] >> shift);
 }
 
 // First run of every tile in the sorted order (tile_first[ntiles] = nruns):
@@ -720,6 +746,37 @@ int sort_runs(unsigned long long* key_in, unsigned long long* key_out,
   cudaStreamSynchronize(st);
   cudaFree(tmp);
   return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+// Exclusive prefix sums for the construction (CUB); tmp == nullptr asks for
+// the temporary bytes in *tmp_bytes.
+cudaError_t scan_counts(void* tmp, size_t* tmp_bytes, const int* in, int64_t* out, int n,
+                        cudaStream_t st) {
+  return cub::DeviceScan::ExclusiveScan(tmp, *tmp_bytes, in, out,
+                                        ::cuda::std::plus<int64_t>{}, (int64_t)0, n, st);
+}
+cudaError_t scan_i64(void* tmp, size_t* tmp_bytes, const int64_t* in, int64_t* out, int n,
+                     cudaStream_t st) {
+  return cub::DeviceScan::ExclusiveSum(tmp, *tmp_bytes, in, out, n, st);
+}
+
+void launch_group_slots(const int* nruns, int64_t R, int64_t* gslots, cudaStream_t st) {
+  const int64_t groups = (R + 31) / 32;
+  k_group_slots<<<blocks_for(groups, 256), 256, 0, st>>>(nruns, R, gslots);
+}
+
+void launch_group_entries(const int* gsteps, int groups, int64_t* out, cudaStream_t st) {
+  k_group_entries<<<blocks_for(groups, 256), 256, 0, st>>>(gsteps, groups, out);
+}
+
+void launch_shift_narrow_i32(const int64_t* in, int* out, int64_t n, int shift,
+                             cudaStream_t st) {
+  k_shift_narrow<int><<<blocks_for(n, 256), 256, 0, st>>>(in, out, n, shift);
+}
+
+void launch_shift_i64(const int64_t* in, int64_t* out, int64_t n, int shift,
+                      cudaStream_t st) {
+  k_shift_narrow<int64_t><<<blocks_for(n, 256), 256, 0, st>>>(in, out, n, shift);
 }
 
 void launch_tile_bounds(RunKey rk, const unsigned long long* skey, int64_t nruns,
