@@ -54,7 +54,8 @@ def _desc(**kw):
 
 @pytest.mark.parametrize("bad", [dict(num_cols=1), dict(num_projs=0),
                                  dict(slices_per_pass=3), dict(len_storage=9),
-                                 dict(mode=5), dict(num_slices=0)])
+                                 dict(mode=5), dict(num_slices=0),
+                                 dict(num_cols=32769), dict(num_projs=-1)])
 def test_invalid_descriptors_rejected_on_host(lib, bad):
     theta = np.zeros(10, np.float32)
     h = C.c_void_p()
