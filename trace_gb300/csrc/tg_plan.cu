@@ -374,7 +374,7 @@ float* batch_ptr(tg_plan* p, float* base, int batch_slot) {
   return base + (int64_t)(batch_slot / p->K) * p->g2 * p->K;
 }
 
-// Tile-ordered forward matrix (tg_tiles.cu): runs of each ray inside 64x64
+// Tile-ordered forward matrix (tg_tiles.cu): runs of each ray inside ts x ts
 // tiles, sorted by (tile, chunk-count class, ray) and packed 32 per warp group.
 int build_tiles(tg_plan* p, int* d_nruns) {
   const DevGeom& G = p->G;

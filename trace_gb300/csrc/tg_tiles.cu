@@ -3,8 +3,8 @@
 // The ray-major forward kernel gathers each segment's K reconstruction values
 // through L1/L2: ~1 sector lookup per segment, and at 2048^2 with 8 slices
 // the 134 MB batch no longer stays in L2 next to the streamed matrix. Here
-// the image is cut into ts x ts tiles (ts = 64 by default; 32 or 96 by plan
-// option) and each ray's segment list into runs
+// the image is cut into ts x ts tiles (ts = 64 by default; 32 to 96 in steps
+// of 16 by plan option) and each ray's segment list into runs
 // (consecutive segments inside one tile). One block per tile loads the
 // tile's K-slice reconstruction into shared memory once and walks all runs
 // through it: lane = run, 32 runs of adjacent rays per warp. A lane's
