@@ -282,6 +282,16 @@ int tg_reset_replica(tg_plan* plan);
  * per slice batch, n_iter times. */
 int tg_iterate(tg_plan* plan, int alg, const tg_params* params, int n_iter);
 
+/* tg_iterate, then tg_get_recon into `recon`, the same bits: the
+ * reconstruction of a whole run (the drivers' loop, then WriteRecon). For a
+ * device or mapped host buffer, an FP32 plan without halo slices (not
+ * APMLR) and no per-kernel timers, the last iteration's slice batches are
+ * written out as each one finishes, on a stream of the plan's own, while
+ * the following batches still compute; otherwise the two calls run one
+ * after the other. No counterpart in the reference. */
+int tg_iterate_get_recon(tg_plan* plan, int alg, const tg_params* params, int n_iter,
+                         float* recon, int on_device);
+
 /* Capture each fused iteration of tg_iterate in a CUDA graph (one per
  * reconstruction-buffer parity, re-captured when the algorithm or its
  * parameters change) and replay it. Needs the plan's own stream or a

@@ -38,6 +38,7 @@ EXPORTED = [
     "tg_plan_get_timing", "tg_plan_set_graphs", "tg_batch_create",
     "tg_batch_iterate", "tg_batch_synchronize", "tg_batch_destroy",
     "tg_batch_last_error", "tg_batch_get_info", "tg_host_alloc", "tg_host_free",
+    "tg_iterate_get_recon",
 ]
 
 
@@ -308,9 +309,25 @@ class Plan:
         return out
 
     # -- operators
-    def iterate(self, alg, n_iter=1, params=None):
+    def iterate(self, alg, n_iter=1, params=None, out=None):
+        """n_iter fused iterations. With `out` (as for get_recon: a device
+        tensor, or a host array / CPU tensor of [S + 2 halo][C][C] float32),
+        the reconstruction is also written there and returned, the last
+        iteration's slice batches leaving as each one finishes when `out` is
+        device or page-locked memory (tg_iterate_get_recon)."""
         p = params if params is not None else default_params(alg)
-        self._chk(self._lib.tg_iterate(self._h, self._alg(alg), C.byref(p), int(n_iter)))
+        if out is None:
+            self._chk(self._lib.tg_iterate(self._h, self._alg(alg), C.byref(p), int(n_iter)))
+            return None
+        if _is_device(out):
+            self._chk(self._lib.tg_iterate_get_recon(self._h, self._alg(alg), C.byref(p),
+                                                     int(n_iter), _ptr(out), 1))
+            return out
+        n = self.S + 2 * self.halo(alg)
+        out = _host_out(out, (n, self.C, self.C))
+        self._chk(self._lib.tg_iterate_get_recon(self._h, self._alg(alg), C.byref(p),
+                                                 int(n_iter), _ptr(out), 0))
+        return out
 
     def reduce(self, alg, params=None):
         p = params if params is not None else default_params(alg)

@@ -4,6 +4,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <functional>
 #include <map>
 #include <cmath>
 #include <cstdio>
@@ -52,6 +53,11 @@ struct tg_plan {
   bool two = false;
   cudaStream_t st2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // tg_iterate_get_recon: the stream that downloads finished slice batches
+  // during the last iteration, one event per batch, and its join event
+  cudaStream_t st_dl = nullptr;
+  std::vector<cudaEvent_t> ev_batch;
+  cudaEvent_t ev_dl = nullptr;
   float* d_part2 = nullptr;
   float* d_upd2 = nullptr;
   // FP64 mode: double state, factors, total lengths and SIRT's a2
@@ -1041,6 +1047,10 @@ int tg_plan_destroy(tg_plan* p) {
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);
   if (p->st2) cudaStreamDestroy(p->st2);
+  if (p->st_dl) cudaStreamSynchronize(p->st_dl);
+  for (auto ev : p->ev_batch) cudaEventDestroy(ev);
+  if (p->ev_dl) cudaEventDestroy(p->ev_dl);
+  if (p->st_dl) cudaStreamDestroy(p->st_dl);
   if (p->own) cudaStreamDestroy(p->own);
   delete p;
   return TG_OK;
@@ -1218,7 +1228,9 @@ static int half_factors_next(const tg_plan* p, int mode) {
 // the caller flips p->cur and counts the iteration).
 // two_streams: the plan's odd slice batches go to its second stream (forked
 // from and joined back into p->st), except while the per-kernel timers run.
-static void issue_iteration(tg_plan* p, const IterArgs& A0, int mode, bool two_streams) {
+// after_batch(b, s): called once batch b's backprojection is issued on s.
+static void issue_iteration(tg_plan* p, const IterArgs& A0, int mode, bool two_streams,
+                            const std::function<void(int, cudaStream_t)>& after_batch = {}) {
   IterArgs A = A0;
   if (p->tiles && p->d.half_gathers) {
     A.half_tile = 1;
@@ -1252,6 +1264,7 @@ static void issue_iteration(tg_plan* p, const IterArgs& A0, int mode, bool two_s
     else
       launch_backward_staged(A, b, p->d_recon[p->cur], p->d_recon[p->cur ^ 1], upd,
                              nullptr, EPI_UPDATE, s);
+    if (after_batch) after_batch(b, s);
   }
   if (two) {
     cudaEventRecord(p->ev_join, p->st2);
@@ -1333,6 +1346,63 @@ int tg_iterate(tg_plan* p, int alg, const tg_params* prm, int n_iter) {
     ++p->iters_done;
   }
   TG_CUDA(p, cudaGetLastError());
+  return TG_OK;
+}
+
+int tg_iterate_get_recon(tg_plan* p, int alg, const tg_params* prm, int n_iter,
+                         float* recon, int on_device) {
+  if (!p || !recon || n_iter < 0)
+    return p ? fail(p, TG_E_ARG, "null output or bad n_iter") : TG_E_ARG;
+  TG_TRY(iterate_ready(p, alg, prm));
+  const int nuser = p->S + 2 * p->halo;
+  const size_t n = (size_t)nuser * p->g2;
+  float* dst = on_device ? recon : mapped_host_out(recon, n);
+  // Overlapped when the output is device or mapped host memory, the plan
+  // runs FP32 without halo slices and without per-kernel timers; else
+  // iterate, then download.
+  if (n_iter == 0 || !dst || p->halo || p->fp64 || p->timing) {
+    TG_TRY(tg_iterate(p, alg, prm, n_iter));
+    return tg_get_recon(p, alg, recon, on_device);
+  }
+  TG_TRY(tg_iterate(p, alg, prm, n_iter - 1));
+  if (!p->st_dl &&
+      (cudaStreamCreateWithFlags(&p->st_dl, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreateWithFlags(&p->ev_dl, cudaEventDisableTiming) != cudaSuccess)) {
+    cudaGetLastError();
+    return fail(p, TG_E_CUDA, "creating the download stream failed");
+  }
+  while ((int)p->ev_batch.size() < p->nb) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(p, TG_E_CUDA, "creating the batch events failed");
+    }
+    p->ev_batch.push_back(e);
+  }
+  const IterArgs A = make_args(p, alg, prm);
+  const int mode = alg == TG_SIRT ? FWD_SIRT : FWD_RATIO;
+  const float* next = p->d_recon[p->cur ^ 1];
+  // the download stream follows everything issued so far; each batch's
+  // slices go out once its backprojection (the last writer of its slots in
+  // this iteration) is done, while the following batches compute
+  TG_CUDA(p, cudaEventRecord(p->ev_dl, p->st));
+  TG_CUDA(p, cudaStreamWaitEvent(p->st_dl, p->ev_dl, 0));
+  issue_iteration(p, A, mode, true, [&](int b, cudaStream_t s) {
+    const int s0 = b * p->K;
+    const int cnt = std::min(p->K, p->S - s0);
+    if (cnt <= 0) return;
+    cudaEventRecord(p->ev_batch[b], s);
+    cudaStreamWaitEvent(p->st_dl, p->ev_batch[b], 0);
+    launch_recon_unpack(next, dst + (int64_t)s0 * p->g2, cnt, (int)p->g2, p->K,
+                        p->vshift + s0, p->st_dl);
+  });
+  TG_CUDA(p, cudaEventRecord(p->ev_dl, p->st_dl));
+  TG_CUDA(p, cudaStreamWaitEvent(p->st, p->ev_dl, 0));
+  p->cur ^= 1;
+  ++p->iters_done;
+  TG_CUDA(p, cudaGetLastError());
+  // a host reconstruction has been written when the call returns
+  if (!on_device) TG_CUDA(p, cudaStreamSynchronize(p->st));
   return TG_OK;
 }
 
