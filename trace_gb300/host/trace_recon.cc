@@ -284,10 +284,13 @@ void run(const Config& cfg, int alg, float* theta, const float* sino, size_t sin
   auto main_recon_replica = main_recon_space->reduction_objects();
   float init_val = 0.;
   GpuDISPEngine<Space> engine(main_recon_space);
+  HostFloats recon(trace_metadata.recon_count());
   const auto t0 = std::chrono::steady_clock::now();
   if (cfg.fused) {
+    // iterations and download in one call (the last iteration's slice
+    // batches leave as each one finishes)
     tg_params prm{cfg.beta, cfg.beta1, cfg.delta, cfg.delta1, cfg.regw};
-    check(tg_iterate(trace_metadata.plan(), alg, &prm, cfg.iters),
+    check(tg_iterate_get_recon(trace_metadata.plan(), alg, &prm, cfg.iters, recon.data(), 0),
           trace_metadata.plan());
   } else {
     for (int i = 0; i < cfg.iters; ++i) {
@@ -307,9 +310,8 @@ void run(const Config& cfg, int alg, float* theta, const float* sino, size_t sin
       engine.ResetReductionSpaces(init_val);
       slices.ResetMirroredRegionIter();
     }
+    trace_metadata.recon_into(alg, recon.data());
   }
-  HostFloats recon(trace_metadata.recon_count());
-  trace_metadata.recon_into(alg, recon.data());
   const double secs = std::chrono::duration<double>(
                           std::chrono::steady_clock::now() - t0).count();
   const int halo = alg == TG_APMLR ? 1 : 0;
