@@ -368,3 +368,32 @@ def test_forward_block_warps_are_bit_identical(warps):
         outs.append(plan.get_recon("pml"))
         plan.close()
     assert np.array_equal(bits(outs[1]), bits(outs[0]))
+
+
+@pytest.mark.parametrize("case", ["center", "apmlr_inner", "apmlr_top", "apmlr_bottom"])
+def test_fast_tiles_geometry_variants_against_fp64(case):
+    """The measured fast path (16-bit lengths, 8 slices per pass, tile-staged
+    forward, half gathers) with a rotation centre off the middle, and APMLR
+    on slabs of a larger volume (inner, top and bottom: the axial penalty's
+    boundary cases), against the FP64 oracle run on the same slab."""
+    C, P, S = 96, 72, 9
+    th = theta_uniform(P)
+    tabs = O.angle_table(th)
+    from trace_gb300.phantom import ellipse_phantoms
+    center = C / 2 + 3.5 if case == "center" else 0.0
+    alg = "pml" if case == "center" else "apmlr"
+    slab = {"center": (0, S), "apmlr_inner": (9, 40), "apmlr_top": (0, 40),
+            "apmlr_bottom": (31, 40)}[case]
+    sino = O.forward(ellipse_phantoms(C, S, seed=23, texture_sigma=0.02), tabs,
+                     center=center)
+    kw = dict(beta=0.05) if alg == "pml" else dict(beta=0.05, beta1=0.5)
+    ref = O.run(alg, sino, tables=tabs, n_iter=4, precision=O.F64, center=center,
+                slice_id=slab[0], num_total_slices=slab[1], **kw)["recon"]
+    plan = tg.Plan(P, S, C, th, center=center, slice_id=slab[0], num_total_slices=slab[1],
+                   slices_per_pass=8, mode="fast", len_storage="u16", delta_index=True,
+                   forward_tiles=True, half_gathers=True)
+    plan.set_sinogram(sino, apply_abs=True)
+    plan.reset_recon(alg)
+    plan.iterate(alg, 4, tg.default_params(alg, **kw))
+    assert rel_l2(plan.get_recon(alg), ref) < 1e-4, case
+    plan.close()
