@@ -594,7 +594,9 @@ int tg_host_alloc(size_t bytes, void** out) {
   if (!out) return fail(nullptr, TG_E_ARG, "null output");
   *out = nullptr;
   if (bytes == 0) return TG_OK;
-  const cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+  // portable: page-locked for every device's context, as plans on several
+  // devices in one process may share the buffer
+  const cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocPortable);
   if (e != cudaSuccess) {
     cudaGetLastError();
     *out = nullptr;
